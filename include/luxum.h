@@ -1,0 +1,203 @@
+/*
+ * luxum.h -- C ABI of the GB300 FDTD engine (drop-in for Luxum's time-stepping path).
+ *
+ * Plain C: no C++ types, no torch types, no exceptions cross this boundary.  Every call
+ * returns an lx_status (0 = ok); the text of the last failure is available through
+ * lx_last_error(sim) (per handle) or lx_last_error(NULL) (per thread, for calls that
+ * failed before a handle existed).
+ *
+ * What each entry point replaces in the reference (paths are within the Luxum project):
+ *   lx_params / lx_params_init / lx_params_from_yaml
+ *       -> class reader: public members reader.h:50-174, readYAML() reader.cc:68-130,
+ *          checkData() reader.cc:141-162 (the reader constructor reader.cc:55-58 runs both)
+ *   lx_sim_create
+ *       -> grid::grid grid.cc:58-95 (single rank: local = global), maxwell::maxwell
+ *          maxwell.cc:60-148 (constants, PML and plane-wave set-up, plane_wave_initialise
+ *          maxwell.cc:825-929), the vfield/field allocations of the four drivers
+ *          (two_dim.cc:63-68, two_dim_pml.cc:86-106, three_dim.cc:66-72,
+ *          three_dim_pml.cc:92-107) and the CPML profiles k_fn/b_fn/c_fn maxwell.cc:997-1280
+ *   lx_sim_set_cb / lx_sim_set_material
+ *       -> the Cb coefficient set-up of the drivers: Cb = dt/eps0 (two_dim.cc:81,
+ *          two_dim_pml.cc:116, three_dim.cc:54) and the material-file formula
+ *          Cb = dt/(eps0*(1+F*1e6)) (three_dim_pml.cc:109-128, fileio::readHDF5 fileio.cc:224-247)
+ *   lx_sim_step
+ *       -> one iteration of the time loop of maxwell::solve() maxwell.cc:157-174:
+ *          solve_planar two_dim.cc:85-144, solve_planar_pml two_dim_pml.cc:126-188,
+ *          solve3d three_dim.cc:82-196, solve3d_pml three_dim_pml.cc:158-283
+ *          (curl vfield.cc:102-386, TF/SF plane_wave_execute maxwell.cc:194-812,
+ *          point source maxwell.cc:944-979 + drivers, max|E|^2 monitor)
+ *   lx_sim_read_field / lx_sim_write_field / lx_sim_field_shape
+ *       -> field::F of each component (field.h:54, staggered extents field.cc:58-77)
+ *   lx_sim_max_e2
+ *       -> local_max / MPI_Reduce(MAX) of the drivers (two_dim_pml.cc:136,181,
+ *          three_dim_pml.cc:168,266-276)
+ *   lx_sim_set_snapshots / lx_sim_set_hdf5_output / lx_sim_sync
+ *       -> fileio(name,false,grid,field*) + writeHDF5(t) fileio.cc:60-212 and the drivers'
+ *          "t % n == 0" write cadence (two_dim_pml.cc:184, three_dim_pml.cc:279)
+ *
+ * Ownership: the library owns all device memory of a handle; callers own every host
+ * buffer they pass.  Distinct handles may be used from distinct host threads; one handle
+ * must not be used from two threads at once.
+ */
+#ifndef LUXUM_H
+#define LUXUM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__) && defined(LX_BUILDING_LIBRARY)
+#define LX_API __attribute__((visibility("default")))
+#else
+#define LX_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lx_status {
+  LX_OK = 0,
+  LX_ERR_INVALID = 1,     /* bad argument or parameter combination */
+  LX_ERR_UNSUPPORTED = 2, /* a combination the reference cannot run either (see message) */
+  LX_ERR_CUDA = 3,        /* a CUDA call failed */
+  LX_ERR_OOM = 4,         /* device or pinned host allocation failed */
+  LX_ERR_BLOWUP = 5,      /* max|E|^2 became non-finite */
+  LX_ERR_IO = 6,          /* file open/parse/write failure */
+  LX_ERR_STATE = 7        /* call not valid in the handle's current state */
+} lx_status;
+
+/* Storage/compute precision of the fields (engine option; the reference is FP64 only). */
+enum { LX_PREC_FP64 = 0, LX_PREC_FP32 = 1, LX_PREC_FP16S = 2 };
+/* CPML coefficient b: reference form exp(-(sigma/kappa - a)/eps0*dt) (maxwell.cc:1215)
+ * or the textbook form exp(-(sigma/kappa + a)/eps0*dt). */
+enum { LX_CPML_REFERENCE = 0, LX_CPML_STANDARD = 1 };
+/* Point-source waveform: the reference's hard CW source amp*sin(omega*t*dt) with amp and
+ * omega truncated to int (maxwell.h:203,206; three_dim_pml.cc:161-165), or an additive
+ * Gaussian-modulated sine pulse amp*exp(-((t-t0)/tw)^2)*sin(omega*t*dt). */
+enum { LX_SRC_CW_HARD = 0, LX_SRC_PULSE_SOFT = 1 };
+/* Field components, in the reference's vfield order (vfield.cc:58-87). */
+enum { LX_EX = 0, LX_EY = 1, LX_EZ = 2, LX_HX = 3, LX_HY = 4, LX_HZ = 5, LX_ETOTAL = 6 };
+
+/* Mirrors the public members of class reader (reader.h:50-174) in parameters.yaml order,
+ * followed by engine options that have no YAML key in the reference. */
+typedef struct lx_params {
+  /* document 1: "isPlanar" */
+  int isPlanar;
+  /* document 2: "X/Y/Z Length", "X/Y/Z Resolution", "Courant factor", "Number of timesteps" */
+  int Nx, Ny, Nz;
+  double dx, dy, dz;
+  double S;
+  int num_timesteps;
+  /* document 3: "X/Y Number of Procs", "Number of Threads per node".  Validated like
+   * reader::checkData; one GPU holds the whole grid, so they do not split it. */
+  int npX, npY, n_threads;
+  /* document 4: sources */
+  int usePS;
+  int Nx_source, Ny_source, Nz_source;
+  double amp_source, omega_source;
+  int usePW;
+  double kx_pw, ky_pw, kz_pw;
+  double Ex_pw, Ey_pw, Ez_pw;
+  double off_pw;
+  int x1_pw, y1_pw, z1_pw, x2_pw, y2_pw, z2_pw;
+  /* document 5: boundary conditions */
+  int usePML;
+  double d_pml;   /* "Thickness of PML" (metres) */
+  double sigma;   /* "sigma_max/sigma_optimal" (reader::sigma) */
+  double sigma_m; /* "m value of sigma" */
+  double kappa;   /* "kappa max" */
+  double a_max;   /* "max value of a" */
+  double a_m;     /* "m value for a" */
+  /* engine options (defaults from lx_params_init reproduce the reference) */
+  int precision;      /* LX_PREC_* (default FP64) */
+  double pw_sigma;    /* plane-wave pulse width in m^2 (default pow(10,-4)/0.5, maxwell.cc:71) */
+  int cpml_mode;      /* LX_CPML_* (default LX_CPML_REFERENCE) */
+  int source_kind;    /* LX_SRC_* (default LX_SRC_CW_HARD) */
+  double src_t0;      /* LX_SRC_PULSE_SOFT: pulse centre in steps */
+  double src_tw;      /* LX_SRC_PULSE_SOFT: pulse 1/e half-width in steps */
+  int monitor_every;  /* compute max|E|^2 every n steps; 0 = only at the end of each lx_sim_step call */
+} lx_params;
+
+typedef struct lx_sim lx_sim;
+
+/* Fills *p with the reference's defaults for everything not read from YAML. */
+LX_API void lx_params_init(lx_params* p);
+
+/* Parses a Luxum parameters.yaml (five flow-mapping documents, reader.cc:68-130) and runs
+ * the checks of reader::checkData (reader.cc:141-162).  Optional sixth document: engine
+ * options ("precision", "pulse width", "cpml mode", ...). */
+LX_API lx_status lx_params_from_yaml(const char* path, lx_params* p);
+
+/* Validates *p (reader::checkData plus the index ranges the reference reads out of bounds),
+ * allocates all device state (fields zeroed as field.cc:78-85 does) and computes the
+ * constants and CPML profiles exactly as maxwell.cc:60-148 / 997-1280. */
+LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out);
+LX_API void lx_sim_destroy(lx_sim* sim);
+/* Zeroes E, H, psi and |E|^2 and rewinds to step 0 (the state after lx_sim_create); keeps
+ * Cb, probe positions and snapshot outputs, so one handle can run many simulations. */
+LX_API lx_status lx_sim_reset(lx_sim* sim);
+
+/* Sets the Cb update coefficient of E component comp (LX_EX..LX_EZ; planar: LX_EY only)
+ * from n = product of the component's staggered extents host doubles, C order. */
+LX_API lx_status lx_sim_set_cb(lx_sim* sim, int comp, const double* cb, size_t n);
+/* Cb = dt / (eps0 * (1 + F * scale)), the reference's material-file formula
+ * (three_dim_pml.cc:122-128 with scale = 1e6; two_dim_pml.cc:112-113 with scale = 11). */
+LX_API lx_status lx_sim_set_material(lx_sim* sim, int comp, const double* F, size_t n, double scale);
+/* Cb = dt / (eps0 * eps_r) over an index box [lo, hi) of every E component. */
+LX_API lx_status lx_sim_set_eps_box(lx_sim* sim, const int lo[3], const int hi[3], double eps_r);
+
+/* Advances nsteps full Yee steps (H half-step then E half-step).  Blocks until the steps
+ * are enqueued and, when a monitor step falls inside, until max|E|^2 is known. */
+LX_API lx_status lx_sim_step(lx_sim* sim, int nsteps);
+/* Waits for all queued device work and snapshot writes of the handle. */
+LX_API lx_status lx_sim_sync(lx_sim* sim);
+
+/* Staggered extents of a component (field.cc:67-77); absent planar components give 0s. */
+LX_API lx_status lx_sim_field_shape(const lx_sim* sim, int comp, int shape[3]);
+LX_API lx_status lx_sim_read_field(lx_sim* sim, int comp, double* host, size_t n);
+LX_API lx_status lx_sim_write_field(lx_sim* sim, int comp, const double* host, size_t n);
+/* Number of completed steps. */
+LX_API int lx_sim_timestep(const lx_sim* sim);
+/* max over the grid of Ey^2 (planar) or Ex^2+Ey^2+Ez^2 (3D) after the last monitor step. */
+LX_API lx_status lx_sim_max_e2(lx_sim* sim, double* out);
+
+/* Point probes: every step records all six components at each (i,j,k) (0 where a
+ * component's extent does not contain the index).  Replaces earlier probes. */
+LX_API lx_status lx_sim_set_probes(lx_sim* sim, const int* ijk, int nprobes, int capacity_steps);
+/* Copies [nsteps recorded][nprobes][6] doubles; *nsteps_out receives the row count. */
+LX_API lx_status lx_sim_read_probes(lx_sim* sim, double* host, size_t n, int* nsteps_out);
+
+/* Snapshot callback: called from the handle's writer thread, in step order, with a host
+ * buffer valid only during the call. */
+typedef void (*lx_snapshot_fn)(void* user, int timestep, int comp, const double* data,
+                               const int shape[3]);
+/* Every `every` steps (after the E update, when timestep % every == 0, as the drivers'
+ * writeHDF5 cadence), copies the components in comp_mask (bit c = component c, bit 6 =
+ * |E|^2 in the Ez-shaped array of three_dim_pml.cc:266-273) to pinned host memory on a
+ * side stream and hands them to fn.  every = 0 disables. */
+LX_API lx_status lx_sim_set_snapshots(lx_sim* sim, int every, unsigned comp_mask, lx_snapshot_fn fn,
+                               void* user);
+/* Same cadence, written to one HDF5 file per component in the layout of fileio.cc:60-212
+ * (dataset "t=<step>", global staggered dims, native double, contiguous). */
+LX_API lx_status lx_sim_set_hdf5_output(lx_sim* sim, int every, int comp, const char* path);
+
+/* Launch all device work of the handle on this CUDA stream (cudaStream_t) instead of its
+ * own.  NULL restores the handle's own stream. */
+LX_API lx_status lx_sim_set_stream(lx_sim* sim, void* cuda_stream);
+
+/* Counters since creation: device kernels launched, bytes copied host->device and
+ * device->host by the handle. */
+LX_API lx_status lx_sim_counters(const lx_sim* sim, uint64_t* kernels, uint64_t* h2d, uint64_t* d2h);
+
+/* Page-locked host memory for fast transfers (cudaHostAlloc). */
+LX_API lx_status lx_host_alloc(size_t bytes, void** ptr);
+LX_API void lx_host_free(void* ptr);
+
+LX_API const char* lx_last_error(const lx_sim* sim);
+LX_API const char* lx_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LUXUM_H */

@@ -1,0 +1,1078 @@
+// lx_api.cu -- implementation of the C ABI in include/luxum.h.
+//
+// Host code here is compiled with -ffp-contract=off: the constants and CPML profiles are
+// computed with the reference's expressions (maxwell.cc:60-148, 997-1280) and must round
+// the same way on x86-64 and aarch64 hosts.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/luxum.h"
+#include "lx_hdf5.h"
+#include "lx_internal.h"
+#include "lx_kernels.h"
+#include "lx_sim.h"
+
+using lx::PatchSet;
+using lx::Slab;
+
+static thread_local std::string g_err;
+
+namespace lx {
+lx_status set_thread_error(const char* msg, lx_status st) {
+  g_err = msg;
+  return st;
+}
+}  // namespace lx
+
+static lx_status fail(lx_sim* s, lx_status st, const std::string& msg) {
+  if (s) s->err = msg;
+  g_err = msg;
+  return st;
+}
+
+#define CK(...)                                                                                       \
+  do {                                                                                                \
+    cudaError_t e_ = (__VA_ARGS__);                                                                        \
+    if (e_ != cudaSuccess)                                                                            \
+      return fail(s, e_ == cudaErrorMemoryAllocation ? LX_ERR_OOM : LX_ERR_CUDA,                      \
+                  std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_));                              \
+  } while (0)
+
+extern "C" LX_API const char* lx_version(void) { return "luxum-gb300 0.1 (sm_103a)"; }
+
+extern "C" LX_API const char* lx_last_error(const lx_sim* s) { return s ? s->err.c_str() : g_err.c_str(); }
+
+extern "C" LX_API void lx_params_init(lx_params* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->dx = p->dy = p->dz = 1e-3;
+  p->S = 0.5;
+  p->npX = p->npY = p->n_threads = 1;
+  p->precision = LX_PREC_FP64;
+  p->pw_sigma = pow(10, -4) / 0.5;  // maxwell.cc:71
+  p->cpml_mode = LX_CPML_REFERENCE;
+  p->source_kind = LX_SRC_CW_HARD;
+  p->src_tw = 1.0;
+  p->sigma = 0.65;
+  p->sigma_m = 3;
+  p->kappa = 1;
+  p->a_m = 1;
+}
+
+// ------------------------------------------------------------------ validation
+
+// reader::checkData (reader.cc:141-162) plus every index range or division the reference
+// would read out of bounds, divide by zero on, or turn into NaN profiles.
+static lx_status validate(const lx_params* p, std::string& why) {
+  char b[256];
+  if (p->npX < 1 || p->npY < 1) { why = "Number of Procs must be >= 1"; return LX_ERR_INVALID; }
+  if ((p->Nx - 2) % p->npX != 0) {
+    why = "ERROR: Condition-- (Number of points - 2) mod Number of processors --is not satisfied in X-direction";
+    return LX_ERR_INVALID;
+  }
+  if ((p->Ny - 2) % p->npY != 0) {
+    why = "ERROR: Condition-- (Number of points - 2) mod Number of processors --is not satisfied in Y-direction";
+    return LX_ERR_INVALID;
+  }
+  if (p->isPlanar && p->Ny != 1) { why = "ERROR: Please put number of grid points in Y-direction as 1 for planar solutions."; return LX_ERR_INVALID; }
+  if (p->isPlanar && p->npY != 1) { why = "ERROR: Please put number of processors in Y-direction as 1 for planar solutions."; return LX_ERR_INVALID; }
+  if (p->Nx < 3 || p->Nz < 3 || (!p->isPlanar && p->Ny < 3)) { why = "grid must have at least 3 points per used axis"; return LX_ERR_INVALID; }
+  if ((double)p->Nx * (p->isPlanar ? 1 : p->Ny) * p->Nz > 4.0e9) { why = "grid larger than 4e9 cells"; return LX_ERR_INVALID; }
+  if (!(p->dx > 0) || !(p->dz > 0) || (!p->isPlanar && !(p->dy > 0)) || !(p->S > 0)) { why = "resolutions and Courant factor must be > 0"; return LX_ERR_INVALID; }
+  if (p->num_timesteps < 0) { why = "Number of timesteps must be >= 0"; return LX_ERR_INVALID; }
+  if (p->usePW) {
+    if (p->x1_pw < 1 || p->x2_pw > p->Nx - 2 || p->x1_pw > p->x2_pw ||
+        p->z1_pw < 1 || p->z2_pw > p->Nz - 2 || p->z1_pw > p->z2_pw ||
+        (!p->isPlanar && (p->y1_pw < 1 || p->y2_pw > p->Ny - 2 || p->y1_pw > p->y2_pw))) {
+      std::snprintf(b, sizeof b,
+                    "total-field box must satisfy 1 <= x1 <= x2 <= Nx-2 (and y, z alike): the reference indexes "
+                    "plane x1-1 and edits curl cells it never recomputes otherwise (got x %d..%d y %d..%d z %d..%d)",
+                    p->x1_pw, p->x2_pw, p->y1_pw, p->y2_pw, p->z1_pw, p->z2_pw);
+      why = b;
+      return LX_ERR_INVALID;
+    }
+    double hx = p->ky_pw * p->Ez_pw - p->kz_pw * p->Ey_pw;
+    double hy = p->kz_pw * p->Ex_pw - p->kx_pw * p->Ez_pw;
+    double hz = p->kx_pw * p->Ey_pw - p->ky_pw * p->Ex_pw;
+    if (hx == 0 && hy == 0 && hz == 0) { why = "k x E is zero: H direction undefined (maxwell.cc:94-102 divides by |k x E|)"; return LX_ERR_INVALID; }
+    if (!(p->pw_sigma > 0)) { why = "plane-wave pulse width must be > 0"; return LX_ERR_INVALID; }
+  }
+  if (p->usePML) {
+    double d0 = p->d_pml / p->dx, d2 = p->d_pml / p->dz, d1 = p->isPlanar ? 2.0 : p->d_pml / p->dy;
+    if (!(d0 > 1) || !(d1 > 1) || !(d2 > 1)) { why = "Thickness of PML must exceed one cell (the profiles divide by d-1)"; return LX_ERR_INVALID; }
+    if (p->sigma_m != std::floor(p->sigma_m)) {
+      why = "m value of sigma must be an integer: the reference raises a negative base to it outside the layer (NaN profiles)";
+      return LX_ERR_INVALID;
+    }
+  }
+  if (p->usePS) {
+    if (p->source_kind != LX_SRC_CW_HARD && p->source_kind != LX_SRC_PULSE_SOFT) { why = "unknown source kind"; return LX_ERR_INVALID; }
+    if (p->isPlanar && p->source_kind == LX_SRC_CW_HARD) {
+      why = "planar point source: the reference writes E->Vz, which planar grids do not have (vfield.cc:69-71)";
+      return LX_ERR_UNSUPPORTED;
+    }
+    int zext = p->isPlanar ? p->Nz : p->Nz - 1;
+    if (p->Nz_source < 0 || p->Nz_source >= zext) { why = "Source Z Pos outside the Ez extent (the reference does not range-check z)"; return LX_ERR_INVALID; }
+    if (p->source_kind == LX_SRC_PULSE_SOFT && !(p->src_tw > 0)) { why = "pulse width must be > 0"; return LX_ERR_INVALID; }
+  }
+  if (p->precision < LX_PREC_FP64 || p->precision > LX_PREC_FP16S) { why = "unknown precision"; return LX_ERR_INVALID; }
+  if (p->monitor_every < 0) { why = "monitor_every must be >= 0"; return LX_ERR_INVALID; }
+  return LX_OK;
+}
+
+// ------------------------------------------------------------------ profiles (host)
+
+// Position array of sigma_fn/k_fn/a_fn (maxwell.cc:1026-1035): index (+0.5 for H), offset 0.
+static double prof_pos(int i, bool is_E) { return is_E ? (double)(i + 0) : ((double)i + 0.5) + 0; }
+
+struct AxisProf {
+  std::vector<double> kE, bE, cE, kH, bH, cH;
+};
+
+// sigma/k/a/b/c of maxwell.cc:997-1280 for one axis (N global points, spacing delta).
+static void axis_profiles(const lx::Consts& K, int cpml_mode, int N, double delta, AxisProf& out) {
+  const double d = K.d_pml / delta;
+  for (int is_E = 1; is_E >= 0; --is_E) {
+    int n = is_E ? N : N - 1;
+    std::vector<double> sg(n), kk(n), aa(n), bb(n), cc(n);
+    for (int i = 0; i < n; i++) {
+      double temp = prof_pos(i, is_E);
+      double w = 0.0;  // sigma_fn :1038-1040
+      w = (double)(temp <= (d - 1)) * pow((((d - 1) - temp) / (d - 1)), K.m_pml) * K.sigma_max + (double)(temp > (d - 1)) * w;
+      w = (double)(temp >= (N - d)) * pow((temp - N + d) / (d - 1), K.m_pml) * K.sigma_max + (double)(temp < (N - d)) * w;
+      sg[i] = w;
+      w = 1;  // k_fn :1100-1102
+      w = (double)(temp <= (d - 1)) * (pow((((d - 1) - temp) / (d - 1)), K.m_pml) * (K.k_max - 1) + 1) + (double)(temp > (d - 1)) * w;
+      w = (double)(temp >= (N - d)) * (pow((temp - N + d) / (d - 1), K.m_pml) * (K.k_max - 1) + 1) + (double)(temp < (N - d)) * w;
+      kk[i] = w;
+      w = 0.0;  // a_fn :1163-1165
+      w = (double)(temp <= (d - 1)) * pow((temp / (d - 1)), K.ma_pml) * K.a_max + (double)(temp > (d - 1)) * w;
+      w = (double)(temp >= (N - d)) * pow((N - 1 - temp) / (d - 1), K.ma_pml) * K.a_max + (double)(temp < (N - d)) * w;
+      aa[i] = w;
+      // b_fn :1215 (reference sign on a) or the textbook sign
+      if (cpml_mode == LX_CPML_STANDARD)
+        bb[i] = exp(-((sg[i] / kk[i] / K.epsilon0) + (aa[i] / K.epsilon0)) * K.dt);
+      else
+        bb[i] = exp(-((sg[i] / kk[i] / K.epsilon0) - (aa[i] / K.epsilon0)) * K.dt);
+      // c_fn :1271-1278
+      cc[i] = (sg[i] == 0) ? 0.0 : sg[i] / (sg[i] * kk[i] + pow(kk[i], 2) * aa[i]) * (bb[i] - 1);
+    }
+    if (is_E) { out.kE = kk; out.bE = bb; out.cE = cc; }
+    else { out.kH = kk; out.bH = bb; out.cH = cc; }
+  }
+}
+
+// Largest run of cells where neither the E nor the H profile is active -> packed slab.
+static Slab make_slab(const AxisProf& a, int N) {
+  std::vector<char> act(N, 0);
+  for (int u = 0; u < N; u++) act[u] = (a.cE[u] != 0.0 || a.kE[u] != 1.0);
+  for (int u = 0; u < N - 1; u++) act[u] |= (a.cH[u] != 0.0 || a.kH[u] != 1.0);
+  int best_a = 0, best_b = 0, u = 0;
+  while (u < N) {
+    if (act[u]) { u++; continue; }
+    int v = u;
+    while (v < N && !act[v]) v++;
+    if (v - u > best_b - best_a) { best_a = u; best_b = v; }
+    u = v;
+  }
+  Slab s;
+  if (best_b - best_a == 0) { s.lo = N; s.hi0 = N; s.n = N; }  // active everywhere
+  else { s.lo = best_a; s.hi0 = best_b; s.n = best_a + (N - best_b); }
+  return s;
+}
+
+// ------------------------------------------------------------------ TF/SF plane sets
+
+static PatchSet mkset(const lx_sim* s, int axis, int pl0, int pl1, double pos0, double pos1, double sg0, double sg1,
+                      double dir, double neg, double dn, int hcurl, const int lo[3], const int hi[3],
+                      const double off[3]) {
+  PatchSet ps;
+  std::memset(&ps, 0, sizeof ps);
+  ps.axis = axis;
+  ps.plane[0] = pl0;
+  ps.plane[1] = pl1;
+  ps.pos_n[0] = pos0;
+  ps.pos_n[1] = pos1;
+  ps.sign[0] = sg0;
+  ps.sign[1] = sg1;
+  ps.dir = dir;
+  ps.neg = neg;
+  ps.dn = dn;
+  ps.hcurl = hcurl;
+  bool empty = false;
+  for (int b = 0; b < 3; b++) {
+    ps.lo[b] = lo[b];
+    ps.hi[b] = hi[b];
+    ps.off[b] = off[b];
+    if (b != axis && hi[b] < lo[b]) empty = true;
+  }
+  // the wave varies along in-plane axis b when its k component is non-zero (planar: no y term)
+  int run = 1;
+  for (int b = 2; b >= 0; b--) {
+    bool varies = (b != axis) && (s->planar ? (b != 1 && s->k.k[b] != 0.0) : (s->k.k[b] != 0.0));
+    ps.n[b] = varies ? (hi[b] - lo[b] + 1) : 1;
+    ps.stride[b] = varies ? run : 0;
+    run *= ps.n[b];
+  }
+  ps.plane_len = run;
+  ps.active = (!empty && dir != 0.0) ? 1 : 0;
+  return ps;
+}
+
+static void build_sets(lx_sim* s) {
+  const lx::Consts& K = s->k;
+  const int p1 = K.p1, p2 = K.p2, q1 = K.q1, q2 = K.q2, r1 = K.r1, r2 = K.r2;
+  const int sx = K.st[0], ex = K.en[0], sy = K.st[1], ey = K.en[1], sz = K.st[2], ez = K.en[2];
+  const double Ex = K.E_dir[0], Ey = K.E_dir[1], Ez = K.E_dir[2];
+  const double Hx = K.H_dir[0], Hy = K.H_dir[1], Hz = K.H_dir[2];
+  const double dx = K.dx, dy = K.dy, dz = K.dz;
+  std::memset(s->setsH, 0, sizeof s->setsH);
+  std::memset(s->setsE, 0, sizeof s->setsE);
+  if (s->planar) {
+    // maxwell.cc:516-591 (planar, adv curls)
+    { int lo[3] = {sx, 0, 0}, hi[3] = {ex, 0, 0}; double off[3] = {0, 0, 0};
+      s->setsH[0][1] = mkset(s, 2, r1 - 1, r2, r1, r2, +1, -1, Ey, 1, dz, 0, lo, hi, off); }   // :539-553
+    { int lo[3] = {0, 0, sz}, hi[3] = {0, 0, ez}; double off[3] = {0, 0, 0};
+      s->setsH[2][0] = mkset(s, 0, p1 - 1, p2, p1, p2, +1, -1, Ey, 1, dx, 0, lo, hi, off); }   // :519-534
+    { int lo[3] = {0, 0, sz}, hi[3] = {0, 0, ez}; double off[3] = {0, 0, 0};
+      s->setsE[1][1] = mkset(s, 0, p1, p2, p1 - 0.5, p2 + 0.5, -1, +1, Hz, -1, dx, 1, lo, hi, off); }  // :559-572
+    { int lo[3] = {sx, 0, 0}, hi[3] = {ex, 0, 0}; double off[3] = {0, 0, 0};
+      s->setsE[1][0] = mkset(s, 2, r1, r2, r1 - 0.5, r2 + 0.5, -1, +1, Hx, -1, dz, 1, lo, hi, off); }  // :577-590
+  } else {
+    // maxwell.cc:597-701 (E-curl sets for the H update, t - 0.5)
+    { int lo[3] = {sx, 0, sz}, hi[3] = {ex, 0, ez - 1}; double off[3] = {0, 0, 0.5};
+      s->setsH[0][0] = mkset(s, 1, q1 - 1, q2, q1, q2, -1, +1, Ez, 1, dy, 0, lo, hi, off); }  // :642-664
+    { int lo[3] = {sx, sy, 0}, hi[3] = {ex, ey - 1, 0}; double off[3] = {0, 0.5, 0};
+      s->setsH[0][1] = mkset(s, 2, r1 - 1, r2, r1, r2, -1, +1, Ey, 1, dz, 0, lo, hi, off); }  // :678-700
+    { int lo[3] = {sx, sy, 0}, hi[3] = {ex - 1, ey, 0}; double off[3] = {0.5, 0, 0};
+      s->setsH[1][0] = mkset(s, 2, r1 - 1, r2, r1, r2, -1, +1, Ex, 1, dz, 0, lo, hi, off); }  // :671-692
+    { int lo[3] = {0, sy, sz}, hi[3] = {0, ey, ez - 1}; double off[3] = {0, 0, 0.5};
+      s->setsH[1][1] = mkset(s, 0, p1 - 1, p2, p1, p2, -1, +1, Ez, 1, dx, 0, lo, hi, off); }  // :607-628
+    { int lo[3] = {0, sy, sz}, hi[3] = {0, ey - 1, ez}; double off[3] = {0, 0.5, 0};
+      s->setsH[2][0] = mkset(s, 0, p1 - 1, p2, p1, p2, -1, +1, Ey, 1, dx, 0, lo, hi, off); }  // :600-621
+    { int lo[3] = {sx, 0, sz}, hi[3] = {ex - 1, 0, ez}; double off[3] = {0.5, 0, 0};
+      s->setsH[2][1] = mkset(s, 1, q1 - 1, q2, q1, q2, -1, +1, Ex, 1, dy, 0, lo, hi, off); }  // :635-656
+    // maxwell.cc:707-809 (H-curl sets for the E update, t)
+    { int lo[3] = {sx, 0, sz}, hi[3] = {ex - 1, 0, ez}; double off[3] = {0.5, 0, 0};
+      s->setsE[0][0] = mkset(s, 1, q1, q2, q1 - 0.5, q2 + 0.5, -1, +1, Hz, 1, dy, 1, lo, hi, off); }  // :743-764
+    { int lo[3] = {sx, sy, 0}, hi[3] = {ex - 1, ey, 0}; double off[3] = {0.5, 0, 0};
+      s->setsE[0][1] = mkset(s, 2, r1, r2, r1 - 0.5, r2 + 0.5, -1, +1, Hy, 1, dz, 1, lo, hi, off); }  // :779-800
+    { int lo[3] = {sx, sy, 0}, hi[3] = {ex, ey - 1, 0}; double off[3] = {0, 0.5, 0};
+      s->setsE[1][0] = mkset(s, 2, r1, r2, r1 - 0.5, r2 + 0.5, -1, +1, Hx, 1, dz, 1, lo, hi, off); }  // :786-807
+    { int lo[3] = {0, sy, sz}, hi[3] = {0, ey - 1, ez}; double off[3] = {0, 0.5, 0};
+      s->setsE[1][1] = mkset(s, 0, p1, p2, p1 - 0.5, p2 + 0.5, -1, +1, Hz, 1, dx, 1, lo, hi, off); }  // :708-729
+    { int lo[3] = {0, sy, sz}, hi[3] = {0, ey, ez - 1}; double off[3] = {0, 0, 0.5};
+      s->setsE[2][0] = mkset(s, 0, p1, p2, p1 - 0.5, p2 + 0.5, -1, +1, Hy, 1, dx, 1, lo, hi, off); }  // :715-736
+    { int lo[3] = {sx, 0, sz}, hi[3] = {ex, 0, ez - 1}; double off[3] = {0, 0, 0.5};
+      s->setsE[2][1] = mkset(s, 1, q1, q2, q1 - 0.5, q2 + 0.5, -1, +1, Hx, 1, dy, 1, lo, hi, off); }  // :750-771
+  }
+  int off = 0;
+  for (int h = 0; h < 2; h++)
+    for (int c = 0; c < 3; c++)
+      for (int part = 0; part < 2; part++) {
+        PatchSet& ps = h == 0 ? s->setsH[c][part] : s->setsE[c][part];
+        if (!ps.active) continue;
+        ps.tab = off;
+        off += 2 * ps.plane_len;
+      }
+  s->tab_total = off;
+}
+
+// plane_wave_initialise maxwell.cc:825-913 for one axis
+static void pw_clip(int a1, int a2, int cs, int ce, int* st, int* en) {
+  if (a1 > ce) { *st = -1; *en = -1; }
+  else if (a1 >= cs) { *st = a1; *en = (a2 > ce) ? ce : a2; }
+  else if (a2 > ce) { *st = cs; *en = ce; }
+  else if (a2 >= cs) { *st = cs; *en = a2; }
+  else { *st = -1; *en = -1; }
+}
+
+// ------------------------------------------------------------------ create / destroy
+
+static size_t elsize(int prec) { return prec == LX_PREC_FP64 ? 8 : (prec == LX_PREC_FP32 ? 4 : 2); }
+
+template <class C>
+static lx_status upload_vec(lx_sim* s, void** dst, const std::vector<double>& v) {
+  std::vector<C> tmp(v.size());
+  for (size_t q = 0; q < v.size(); q++) tmp[q] = (C)v[q];
+  CK(cudaMalloc(dst, tmp.size() * sizeof(C) + 16));
+  CK(cudaMemcpy(*dst, tmp.data(), tmp.size() * sizeof(C), cudaMemcpyHostToDevice));
+  s->n_h2d += tmp.size() * sizeof(C);
+  return LX_OK;
+}
+
+static void compute_extents(lx_sim* s) {
+  const int Nx = s->Nx, Ny = s->Ny, Nz = s->Nz;
+  std::memset(s->ext, 0, sizeof s->ext);
+  if (s->planar) {
+    int ey[3] = {Nx, 1, Nz}, hx[3] = {Nx, 1, Nz - 1}, hz[3] = {Nx - 1, 1, Nz};  // vfield.cc:64-70
+    std::memcpy(s->ext[LX_EY], ey, sizeof ey);
+    std::memcpy(s->ext[LX_HX], hx, sizeof hx);
+    std::memcpy(s->ext[LX_HZ], hz, sizeof hz);
+  } else {
+    int e[6][3] = {{Nx - 1, Ny, Nz}, {Nx, Ny - 1, Nz}, {Nx, Ny, Nz - 1},      // vfield.cc:81-83
+                   {Nx, Ny - 1, Nz - 1}, {Nx - 1, Ny, Nz - 1}, {Nx - 1, Ny - 1, Nz}};  // vfield.cc:76-78
+    std::memcpy(s->ext, e, sizeof e);
+    s->ext[LX_ETOTAL][0] = Nx;
+    s->ext[LX_ETOTAL][1] = Ny;
+    s->ext[LX_ETOTAL][2] = Nz - 1;
+  }
+}
+
+static size_t ext_n(const lx_sim* s, int c) { return (size_t)s->ext[c][0] * s->ext[c][1] * s->ext[c][2]; }
+
+static void stop_writer(lx_sim* s);
+
+extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
+  if (!s) return;
+  stop_writer(s);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (int c = 0; c < 3; c++) {
+    cudaFree(s->E[c]); cudaFree(s->H[c]); cudaFree(s->Cbs[c]);
+    for (int q = 0; q < 6; q++) cudaFree(s->prof[c][q]);
+    for (int q = 0; q < 2; q++) { cudaFree(s->psiH[c][q]); cudaFree(s->psiE[c][q]); }
+  }
+  cudaFree(s->tab); cudaFree(s->d_max); cudaFree(s->etotal); cudaFree(s->xfer);
+  cudaFree(s->d_probe_ijk); cudaFree(s->d_probe);
+  for (auto& sl : s->slots) {
+    cudaFree(sl.dev);
+    if (sl.host) cudaFreeHost(sl.host);
+    if (sl.ev_d2h) cudaEventDestroy(sl.ev_d2h);
+  }
+  for (auto& o : s->outputs) delete o.h5;
+  if (s->own) cudaStreamDestroy(s->own);
+  if (s->side) cudaStreamDestroy(s->side);
+  delete s;
+}
+
+static lx_status alloc_zero(lx_sim* s, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) return LX_OK;
+  CK(cudaMalloc(p, bytes));
+  CK(cudaMemsetAsync(*p, 0, bytes, s->stream));
+  return LX_OK;
+}
+
+template <class C>
+static lx_status create_typed(lx_sim* s) {
+  const lx::Consts& K = s->k;
+  const size_t fb = s->ncell * s->tsize;
+  lx_status st;
+  // fields (field.cc:77-85 zero-initialises every component)
+  for (int c = 0; c < 3; c++) {
+    if (s->planar && c != 1) continue;
+    if ((st = alloc_zero(s, &s->E[c], fb))) return st;
+    if ((st = alloc_zero(s, &s->Cbs[c], s->ncell * sizeof(C)))) return st;
+  }
+  for (int c = 0; c < 3; c++) {
+    if (s->planar && c == 1) continue;
+    if ((st = alloc_zero(s, &s->H[c], fb))) return st;
+  }
+  // Cb = dt/epsilon0 (two_dim.cc:81, two_dim_pml.cc:116, three_dim.cc:54)
+  s->cb0 = K.dt / K.epsilon0;
+  for (int c = 0; c < 3; c++) {
+    if (!s->Cbs[c]) continue;
+    int lo[3] = {0, 0, 0}, hi[3] = {s->ext[c][0], s->ext[c][1], s->ext[c][2]};
+    CK(lx::launch_eps_box<C>((C*)s->Cbs[c], s->ext[c], s->Ny, s->Nzp, lo, hi, s->cb0 * s->cbs_scale, s->stream));
+    s->n_kernels++;
+  }
+  // CPML profiles and slabs
+  if (s->pml) {
+    for (int a = 0; a < 3; a++) {
+      if (s->planar && a == 1) continue;
+      const int N = a == 0 ? s->p.Nx : (a == 1 ? s->p.Ny : s->p.Nz);
+      const double delta = a == 0 ? s->p.dx : (a == 1 ? s->p.dy : s->p.dz);
+      AxisProf ap;
+      axis_profiles(K, s->p.cpml_mode, N, delta, ap);
+      s->slab[a] = make_slab(ap, N);
+      std::vector<double> rkE(ap.kE.size()), rkH(ap.kH.size());
+      for (size_t q = 0; q < rkE.size(); q++) rkE[q] = 1.0 / ap.kE[q];
+      for (size_t q = 0; q < rkH.size(); q++) rkH[q] = 1.0 / ap.kH[q];
+      if ((st = upload_vec<C>(s, &s->prof[a][0], ap.bE))) return st;
+      if ((st = upload_vec<C>(s, &s->prof[a][1], ap.cE))) return st;
+      if ((st = upload_vec<C>(s, &s->prof[a][2], rkE))) return st;
+      if ((st = upload_vec<C>(s, &s->prof[a][3], ap.bH))) return st;
+      if ((st = upload_vec<C>(s, &s->prof[a][4], ap.cH))) return st;
+      if ((st = upload_vec<C>(s, &s->prof[a][5], rkH))) return st;
+    }
+    // psi arrays: [component][part] -> axis of that part's derivative
+    const int axH[3][2] = {{1, 2}, {2, 0}, {0, 1}};  // Hx: d/dy, d/dz; Hy: d/dz, d/dx; Hz: d/dx, d/dy
+    const int axE[3][2] = {{1, 2}, {2, 0}, {0, 1}};  // Ex: d/dy, d/dz; Ey: d/dz, d/dx; Ez: d/dx, d/dy
+    auto psi_size = [&](int axis) -> size_t {
+      const Slab& sl = s->slab[axis];
+      if (sl.n == 0) return 0;
+      if (axis == 0) return (size_t)sl.n * s->Ny * s->Nzp;
+      if (axis == 1) return (size_t)s->Nx * sl.n * s->Nzp;
+      return (size_t)s->Nx * s->Ny * sl.n;
+    };
+    for (int c = 0; c < 3; c++)
+      for (int part = 0; part < 2; part++) {
+        bool useH = !s->planar || (c == 0 && part == 1) || (c == 2 && part == 0);
+        bool useE = !s->planar || (c == 1);
+        if (s->planar && (axH[c][part] == 1)) useH = false;
+        if (s->planar && (axE[c][part] == 1)) useE = false;
+        if (useH) {
+          s->psiH_n[c][part] = psi_size(axH[c][part]);
+          if ((st = alloc_zero(s, &s->psiH[c][part], s->psiH_n[c][part] * sizeof(C)))) return st;
+        }
+        if (useE) {
+          s->psiE_n[c][part] = psi_size(axE[c][part]);
+          if ((st = alloc_zero(s, &s->psiE[c][part], s->psiE_n[c][part] * sizeof(C)))) return st;
+        }
+      }
+  }
+  if (s->tfsf) {
+    build_sets(s);
+    CK(cudaMalloc(&s->tab, (size_t)(s->tab_total > 0 ? s->tab_total : 1) * sizeof(C)));
+  }
+  CK(cudaMalloc(&s->d_max, 64));
+  CK(cudaMemsetAsync(s->d_max, 0, 64, s->stream));
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
+  if (!p || !out) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  *out = nullptr;
+  std::string why;
+  lx_status st = validate(p, why);
+  if (st) return fail(nullptr, st, why);
+  lx_sim* s = new (std::nothrow) lx_sim();
+  if (!s) return fail(nullptr, LX_ERR_OOM, "host allocation failed");
+  s->p = *p;
+  s->planar = p->isPlanar != 0;
+  s->pml = p->usePML != 0;
+  s->tfsf = p->usePW != 0;
+  s->prec = p->precision;
+  s->tsize = elsize(p->precision);
+  s->csize = p->precision == LX_PREC_FP64 ? 8 : 4;
+  // grid::grid grid.cc:83-93, single rank
+  s->Nx = (p->Nx - 2) / 1 + 2;
+  s->Ny = s->planar ? 1 : (p->Ny - 2) / 1 + 2;
+  s->Nz = p->Nz;
+  const int per = (int)(128 / s->tsize);
+  s->Nzp = (s->Nz + per - 1) / per * per;
+  s->ncell = (size_t)s->Nx * s->Ny * s->Nzp;
+  compute_extents(s);
+
+  // maxwell::maxwell maxwell.cc:60-148
+  lx::Consts& K = s->k;
+  std::memset(&K, 0, sizeof K);
+  K.epsilon0 = 8.85 * pow(10, -12);
+  K.mew0 = M_PI * 4 * pow(10, -7);
+  K.S = p->S;
+  K.c = 1 / pow(K.epsilon0 * K.mew0, 0.5);
+  K.dt = K.S * p->dx / K.c;
+  K.dx = p->dx;
+  K.dy = p->dy;
+  K.dz = p->dz;
+  K.sigma = p->pw_sigma;
+  K.init = p->off_pw;
+  if (s->pml) {
+    K.a_max = p->a_max;
+    K.k_max = p->kappa;
+    K.m_pml = p->sigma_m;
+    K.ma_pml = p->a_m;
+    K.sigma_optimal = 0.8 * (K.m_pml + 1) / K.dx / pow(K.mew0 / K.epsilon0, 0.5);
+    K.sigma_max = K.sigma_optimal * p->sigma;
+    K.d_pml = p->d_pml;
+  }
+  if (s->tfsf) {
+    K.E_dir[0] = p->Ex_pw; K.E_dir[1] = p->Ey_pw; K.E_dir[2] = p->Ez_pw;
+    K.k[0] = p->kx_pw; K.k[1] = p->ky_pw; K.k[2] = p->kz_pw;
+    K.H_dir[0] = K.k[1] * K.E_dir[2] - K.k[2] * K.E_dir[1];
+    K.H_dir[1] = K.k[2] * K.E_dir[0] - K.k[0] * K.E_dir[2];
+    K.H_dir[2] = K.k[0] * K.E_dir[1] - K.k[1] * K.E_dir[0];
+    double H_abs = pow(pow(K.H_dir[0], 2) + pow(K.H_dir[1], 2) + pow(K.H_dir[2], 2), 0.5);
+    for (int a = 0; a < 3; a++) K.H_dir[a] = K.H_dir[a] / H_abs;
+    K.p1 = p->x1_pw; K.q1 = p->y1_pw; K.r1 = p->z1_pw;
+    K.p2 = p->x2_pw; K.q2 = p->y2_pw; K.r2 = p->z2_pw;
+    pw_clip(K.p1, K.p2, 0, s->Nx - 1, &K.st[0], &K.en[0]);
+    if (s->planar) pw_clip(K.q1, K.q2, 0, 0, &K.st[1], &K.en[1]);
+    else pw_clip(K.q1, K.q2, 0, s->Ny - 1, &K.st[1], &K.en[1]);
+    pw_clip(K.r1, K.r2, 0, s->Nz - 1, &K.st[2], &K.en[2]);
+  }
+  s->uniform = s->planar ? (p->dx == p->dz) : (p->dx == p->dy && p->dx == p->dz);
+  s->cbs_scale = s->uniform ? 1.0 / p->dx : 1.0;
+
+  // point source: check_global_limits (maxwell.cc:944-959) skips it silently off the grid
+  if (p->usePS) {
+    int x = p->Nx_source, y = s->planar ? 0 : p->Ny_source, z = p->Nz_source;
+    bool inside = x >= 0 && y >= 0 && x <= s->Nx - 1 && y <= (s->planar ? 0 : s->Ny - 1);
+    if (inside) {
+      s->src_kind = p->source_kind == LX_SRC_CW_HARD ? 0 : 1;
+      s->src_idx = ((long long)x * s->Ny + y) * s->Nzp + z;
+    }
+  }
+
+  cudaError_t e = cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    std::string m = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+    lx_sim_destroy(s);
+    return fail(nullptr, LX_ERR_CUDA, m);
+  }
+  s->stream = s->own;
+  st = (s->csize == 8) ? create_typed<double>(s) : create_typed<float>(s);
+  if (st == LX_OK) {
+    e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) st = fail(s, LX_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
+  }
+  if (st) {
+    std::string m = s->err;
+    lx_sim_destroy(s);
+    return fail(nullptr, st, m);
+  }
+  *out = s;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_reset(lx_sim* s) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  const size_t fb = s->ncell * s->tsize;
+  for (int c = 0; c < 3; c++) {
+    if (s->E[c]) CK(cudaMemsetAsync(s->E[c], 0, fb, s->stream));
+    if (s->H[c]) CK(cudaMemsetAsync(s->H[c], 0, fb, s->stream));
+    for (int q = 0; q < 2; q++) {
+      if (s->psiH[c][q]) CK(cudaMemsetAsync(s->psiH[c][q], 0, s->psiH_n[c][q] * s->csize, s->stream));
+      if (s->psiE[c][q]) CK(cudaMemsetAsync(s->psiE[c][q], 0, s->psiE_n[c][q] * s->csize, s->stream));
+    }
+  }
+  if (s->etotal) CK(cudaMemsetAsync(s->etotal, 0, s->ncell * s->csize, s->stream));
+  s->t = 0;
+  s->probe_rows = 0;
+  s->last_max = 0.0;
+  return LX_OK;
+}
+
+// ------------------------------------------------------------------ transfers
+
+static lx_status ensure_xfer(lx_sim* s) {
+  if (s->xfer) return LX_OK;
+  size_t m = 0;
+  for (int c = 0; c < 7; c++) m = std::max(m, ext_n(s, c));
+  CK(cudaMalloc(&s->xfer, m * sizeof(double) + 64));
+  s->xfer_cap = m;
+  return LX_OK;
+}
+
+static void* comp_ptr(lx_sim* s, int comp) {
+  if (comp >= LX_EX && comp <= LX_EZ) return s->E[comp];
+  if (comp >= LX_HX && comp <= LX_HZ) return s->H[comp - 3];
+  if (comp == LX_ETOTAL) return s->etotal;
+  return nullptr;
+}
+
+static lx_status gather(lx_sim* s, int comp, double* dst) {
+  void* src = comp_ptr(s, comp);
+  if (comp == LX_ETOTAL) {
+    // |E|^2 is kept in compute precision
+    if (s->csize == 8) CK(lx::launch_gather<double>((const double*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+    else CK(lx::launch_gather<float>((const float*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+  } else if (s->prec == LX_PREC_FP64) {
+    CK(lx::launch_gather<double>((const double*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+  } else if (s->prec == LX_PREC_FP32) {
+    CK(lx::launch_gather<float>((const float*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+  } else {
+    CK(lx::launch_gather<__half>((const __half*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+  }
+  s->n_kernels++;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_field_shape(const lx_sim* s, int comp, int shape[3]) {
+  if (!s || !shape || comp < 0 || comp > LX_ETOTAL) return fail((lx_sim*)s, LX_ERR_INVALID, "bad component");
+  for (int a = 0; a < 3; a++) shape[a] = s->ext[comp][a];
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_read_field(lx_sim* s, int comp, double* host, size_t n) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  if (comp < 0 || comp > LX_ETOTAL) return fail(s, LX_ERR_INVALID, "bad component");
+  const size_t m = ext_n(s, comp);
+  if (n != m) return fail(s, LX_ERR_INVALID, "buffer size does not match the component's staggered extent");
+  if (m == 0) return LX_OK;
+  if (comp == LX_ETOTAL && !s->etotal) return fail(s, LX_ERR_STATE, "|E|^2 is only kept when a snapshot asks for it");
+  lx_status st = ensure_xfer(s);
+  if (st) return st;
+  if ((st = gather(s, comp, s->xfer))) return st;
+  CK(cudaMemcpyAsync(host, s->xfer, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_d2h += m * sizeof(double);
+  return LX_OK;
+}
+
+static lx_status scatter(lx_sim* s, int comp, void* dst, bool compute_prec, int mode, double a, double scale) {
+  const int* ext = s->ext[comp];
+  if (compute_prec || s->prec == LX_PREC_FP64 || s->prec == LX_PREC_FP32) {
+    bool dbl = compute_prec ? s->csize == 8 : s->prec == LX_PREC_FP64;
+    if (dbl) CK(lx::launch_scatter<double>(s->xfer, (double*)dst, ext, s->Ny, s->Nzp, mode, a, s->k.dt, s->k.epsilon0, scale, s->stream));
+    else CK(lx::launch_scatter<float>(s->xfer, (float*)dst, ext, s->Ny, s->Nzp, mode, a, s->k.dt, s->k.epsilon0, scale, s->stream));
+  } else {
+    CK(lx::launch_scatter<__half>(s->xfer, (__half*)dst, ext, s->Ny, s->Nzp, mode, a, s->k.dt, s->k.epsilon0, scale, s->stream));
+  }
+  s->n_kernels++;
+  return LX_OK;
+}
+
+static lx_status upload(lx_sim* s, const double* host, size_t m) {
+  lx_status st = ensure_xfer(s);
+  if (st) return st;
+  CK(cudaMemcpyAsync(s->xfer, host, m * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  s->n_h2d += m * sizeof(double);
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_write_field(lx_sim* s, int comp, const double* host, size_t n) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  if (comp < 0 || comp > LX_HZ) return fail(s, LX_ERR_INVALID, "bad component");
+  const size_t m = ext_n(s, comp);
+  if (n != m) return fail(s, LX_ERR_INVALID, "buffer size does not match the component's staggered extent");
+  if (m == 0) return LX_OK;
+  lx_status st = upload(s, host, m);
+  if (st) return st;
+  if ((st = scatter(s, comp, comp_ptr(s, comp), false, 0, 1.0, 0.0))) return st;
+  CK(cudaStreamSynchronize(s->stream));
+  return LX_OK;
+}
+
+static lx_status check_cb_comp(lx_sim* s, int comp, size_t n) {
+  if (comp < LX_EX || comp > LX_EZ || !s->Cbs[comp]) return fail(s, LX_ERR_INVALID, "Cb exists for Ex, Ey, Ez (planar: Ey only)");
+  if (n != ext_n(s, comp)) return fail(s, LX_ERR_INVALID, "buffer size does not match the component's staggered extent");
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_set_cb(lx_sim* s, int comp, const double* cb, size_t n) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx_status st = check_cb_comp(s, comp, n);
+  if (st) return st;
+  if ((st = upload(s, cb, n))) return st;
+  if ((st = scatter(s, comp, s->Cbs[comp], true, 1, s->cbs_scale, 0.0))) return st;
+  CK(cudaStreamSynchronize(s->stream));
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_set_material(lx_sim* s, int comp, const double* F, size_t n, double scale) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx_status st = check_cb_comp(s, comp, n);
+  if (st) return st;
+  if ((st = upload(s, F, n))) return st;
+  if ((st = scatter(s, comp, s->Cbs[comp], true, 2, s->cbs_scale, scale))) return st;
+  CK(cudaStreamSynchronize(s->stream));
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_set_eps_box(lx_sim* s, const int lo[3], const int hi[3], double eps_r) {
+  if (!s || !lo || !hi) return fail(s, LX_ERR_INVALID, "null argument");
+  if (!(eps_r > 0)) return fail(s, LX_ERR_INVALID, "eps_r must be > 0");
+  const double val = s->k.dt / (s->k.epsilon0 * eps_r) * s->cbs_scale;
+  for (int c = 0; c < 3; c++) {
+    if (!s->Cbs[c]) continue;
+    if (s->csize == 8) CK(lx::launch_eps_box<double>((double*)s->Cbs[c], s->ext[c], s->Ny, s->Nzp, lo, hi, val, s->stream));
+    else CK(lx::launch_eps_box<float>((float*)s->Cbs[c], s->ext[c], s->Ny, s->Nzp, lo, hi, val, s->stream));
+    s->n_kernels++;
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  return LX_OK;
+}
+
+// ------------------------------------------------------------------ probes
+
+extern "C" LX_API lx_status lx_sim_set_probes(lx_sim* s, const int* ijk, int nprobes, int cap) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  if (nprobes < 0 || nprobes > lx::kMaxProbes || cap < 0) return fail(s, LX_ERR_INVALID, "0..64 probes, capacity >= 0");
+  CK(cudaStreamSynchronize(s->stream));
+  cudaFree(s->d_probe_ijk);
+  cudaFree(s->d_probe);
+  s->d_probe_ijk = nullptr;
+  s->d_probe = nullptr;
+  s->nprobes = 0;
+  s->probe_cap = 0;
+  s->probe_rows = 0;
+  if (nprobes == 0 || cap == 0) return LX_OK;
+  CK(cudaMalloc(&s->d_probe_ijk, sizeof(int) * 3 * nprobes));
+  CK(cudaMemcpy(s->d_probe_ijk, ijk, sizeof(int) * 3 * nprobes, cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&s->d_probe, sizeof(double) * 6 * (size_t)nprobes * cap));
+  CK(cudaMemset(s->d_probe, 0, sizeof(double) * 6 * (size_t)nprobes * cap));
+  s->nprobes = nprobes;
+  s->probe_cap = cap;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_read_probes(lx_sim* s, double* host, size_t n, int* rows) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  const size_t m = (size_t)s->probe_rows * s->nprobes * 6;
+  if (rows) *rows = s->probe_rows;
+  if (n < m) return fail(s, LX_ERR_INVALID, "probe buffer too small");
+  if (m == 0) return LX_OK;
+  CK(cudaMemcpyAsync(host, s->d_probe, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_d2h += m * sizeof(double);
+  return LX_OK;
+}
+
+// ------------------------------------------------------------------ snapshots
+
+static void writer_main(lx_sim* s) {
+  cudaSetDevice(0);
+  for (;;) {
+    lx::SnapJob job;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv.wait(lk, [&] { return s->stop || !s->jobs.empty(); });
+      if (s->jobs.empty() && s->stop) return;
+      job = s->jobs.front();
+      s->jobs.pop_front();
+    }
+    lx::SnapSlot& sl = s->slots[job.slot];
+    cudaError_t e = cudaEventSynchronize(sl.ev_d2h);
+    std::string err;
+    if (e != cudaSuccess) err = std::string("snapshot copy: ") + cudaGetErrorString(e);
+    if (err.empty()) {
+      for (auto& o : s->outputs) {
+        if (o.every <= 0 || job.t % o.every != 0) continue;
+        for (int c = 0; c < 7; c++) {
+          if (!(o.mask & (1u << c)) || !(job.mask & (1u << c))) continue;
+          const double* data = sl.host + job.off[c];
+          if (o.fn) o.fn(o.user, job.t, c, data, s->ext[c]);
+          if (o.h5) {
+            std::string m = o.h5->write(job.t, data);
+            if (!m.empty() && err.empty()) err = m;
+          }
+        }
+      }
+    }
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      sl.busy = false;
+      s->pending--;
+      if (!err.empty() && s->writer_err.empty()) s->writer_err = err;
+    }
+    s->cv.notify_all();
+  }
+}
+
+static void stop_writer(lx_sim* s) {
+  if (!s->writer_on) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  s->writer.join();
+  s->writer_on = false;
+  s->stop = false;
+}
+
+static lx_status add_output(lx_sim* s, const lx::Output& o) {
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  s->outputs.push_back(o);
+  // size the staging slots for the union of all outputs' components
+  unsigned all = 0;
+  for (auto& q : s->outputs) all |= q.mask;
+  size_t need = 0;
+  for (int c = 0; c < 7; c++)
+    if (all & (1u << c)) need += ext_n(s, c);
+  for (auto& sl : s->slots) {
+    if (sl.cap >= need) continue;
+    cudaFree(sl.dev);
+    if (sl.host) cudaFreeHost(sl.host);
+    sl.dev = nullptr;
+    sl.host = nullptr;
+    CK(cudaMalloc(&sl.dev, need * sizeof(double)));
+    CK(cudaHostAlloc(&sl.host, need * sizeof(double), cudaHostAllocDefault));
+    if (!sl.ev_d2h) CK(cudaEventCreateWithFlags(&sl.ev_d2h, cudaEventDisableTiming));
+    sl.cap = need;
+  }
+  if ((all & (1u << LX_ETOTAL)) && !s->etotal) {
+    if (s->planar) return fail(s, LX_ERR_INVALID, "|E|^2 snapshots exist for 3-D grids only");
+    CK(cudaMalloc(&s->etotal, s->ncell * s->csize));
+    CK(cudaMemset(s->etotal, 0, s->ncell * s->csize));
+  }
+  if (!s->writer_on) {
+    s->writer = std::thread(writer_main, s);
+    s->writer_on = true;
+  }
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_set_snapshots(lx_sim* s, int every, unsigned mask, lx_snapshot_fn fn, void* user) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  if (every < 0 || (every > 0 && !fn)) return fail(s, LX_ERR_INVALID, "every >= 0 and a callback are required");
+  for (int c = 0; c < 7; c++)
+    if ((mask & (1u << c)) && ext_n(s, c) == 0) return fail(s, LX_ERR_INVALID, "component absent on this grid");
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  for (auto it = s->outputs.begin(); it != s->outputs.end();) {
+    if (it->fn) it = s->outputs.erase(it);
+    else ++it;
+  }
+  if (every == 0) return LX_OK;
+  lx::Output o;
+  o.every = every;
+  o.mask = mask & 0x7f;
+  o.fn = fn;
+  o.user = user;
+  return add_output(s, o);
+}
+
+extern "C" LX_API lx_status lx_sim_set_hdf5_output(lx_sim* s, int every, int comp, const char* path) {
+  if (!s || !path) return fail(s, LX_ERR_INVALID, "null argument");
+  if (every <= 0 || comp < 0 || comp > LX_ETOTAL || ext_n(s, comp) == 0) return fail(s, LX_ERR_INVALID, "bad cadence or component");
+  lx::Output o;
+  o.every = every;
+  o.mask = 1u << comp;
+  o.h5 = new lx::Hdf5Writer();
+  std::string m = o.h5->open(path, s->ext[comp]);
+  if (!m.empty()) {
+    delete o.h5;
+    return fail(s, LX_ERR_IO, m);
+  }
+  o.h5_comp = comp;
+  return add_output(s, o);
+}
+
+// Gathers the due components into a free staging slot and queues the copy to pinned memory.
+static lx_status snapshot(lx_sim* s, int t, unsigned mask) {
+  int slot = -1;
+  {
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv.wait(lk, [&] { return !s->slots[0].busy || !s->slots[1].busy; });
+    slot = !s->slots[0].busy ? 0 : 1;
+    s->slots[slot].busy = true;
+    s->pending++;
+  }
+  lx::SnapSlot& sl = s->slots[slot];
+  lx::SnapJob job;
+  job.slot = slot;
+  job.t = t;
+  job.mask = mask;
+  size_t off = 0;
+  for (int c = 0; c < 7; c++) {
+    job.off[c] = off;
+    if (!(mask & (1u << c))) continue;
+    lx_status st = gather(s, c, sl.dev + off);
+    if (st) return st;
+    off += ext_n(s, c);
+  }
+  // the side stream copies once the gathers on the compute stream are done
+  cudaEvent_t ev;
+  CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  CK(cudaEventRecord(ev, s->stream));
+  CK(cudaStreamWaitEvent(s->side, ev, 0));
+  CK(cudaEventDestroy(ev));
+  CK(cudaMemcpyAsync(sl.host, sl.dev, off * sizeof(double), cudaMemcpyDeviceToHost, s->side));
+  CK(cudaEventRecord(sl.ev_d2h, s->side));
+  // the next gather into this slot must wait for the copy to finish
+  CK(cudaStreamWaitEvent(s->stream, sl.ev_d2h, 0));
+  s->n_d2h += off * sizeof(double);
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->jobs.push_back(job);
+  }
+  s->cv.notify_all();
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_sync(lx_sim* s) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaStreamSynchronize(s->side));
+  std::unique_lock<std::mutex> lk(s->mu);
+  s->cv.wait(lk, [&] { return s->pending == 0; });
+  if (!s->writer_err.empty()) {
+    std::string m = s->writer_err;
+    s->writer_err.clear();
+    lk.unlock();
+    return fail(s, LX_ERR_IO, m);
+  }
+  return LX_OK;
+}
+
+// ------------------------------------------------------------------ stepping
+
+template <class T, class C>
+static lx::StepParams<T, C> step_params(lx_sim* s) {
+  lx::StepParams<T, C> p;
+  std::memset(&p, 0, sizeof p);
+  p.Nx = s->Nx; p.Ny = s->Ny; p.Nz = s->Nz; p.Nzp = s->Nzp;
+  p.sj = s->Nzp;
+  p.si = (long long)s->Ny * s->Nzp;
+  for (int c = 0; c < 3; c++) {
+    p.E[c] = (T*)s->E[c];
+    p.H[c] = (T*)s->H[c];
+    p.Cbs[c] = (const C*)s->Cbs[c];
+  }
+  const double Db = s->k.dt / s->k.mew0;  // Db arrays = dt/mew0 (two_dim_pml.cc:117, three_dim_pml.cc:130-132)
+  p.Dbs = (C)(s->uniform ? Db * (1.0 / s->p.dx) : Db);
+  p.rd[0] = (C)(1.0 / s->p.dx);
+  p.rd[1] = (C)(s->planar ? 0.0 : 1.0 / s->p.dy);
+  p.rd[2] = (C)(1.0 / s->p.dz);
+  p.pml = s->pml;
+  for (int a = 0; a < 3; a++) {
+    p.slab[a] = s->slab[a];
+    if (!s->pml) { p.slab[a].lo = 0; p.slab[a].hi0 = 1 << 30; p.slab[a].n = 0; }
+    p.bE[a] = (const C*)s->prof[a][0];
+    p.cE[a] = (const C*)s->prof[a][1];
+    p.rkE[a] = (const C*)s->prof[a][2];
+    p.bH[a] = (const C*)s->prof[a][3];
+    p.cH[a] = (const C*)s->prof[a][4];
+    p.rkH[a] = (const C*)s->prof[a][5];
+  }
+  if (s->planar) { p.slab[1].lo = 0; p.slab[1].hi0 = 1 << 30; p.slab[1].n = 0; }
+  for (int c = 0; c < 3; c++)
+    for (int q = 0; q < 2; q++) {
+      p.psiH[c][q] = (C*)s->psiH[c][q];
+      p.psiE[c][q] = (C*)s->psiE[c][q];
+      p.setsH[c][q] = s->setsH[c][q];
+      p.setsE[c][q] = s->setsE[c][q];
+    }
+  p.tfsf = s->tfsf && s->tab_total > 0;
+  p.tab = (const C*)s->tab;
+  return p;
+}
+
+template <class T, class C>
+static lx_status run_steps(lx_sim* s, int nsteps) {
+  lx::StepParams<T, C> sp = step_params<T, C>(s);
+  lx::PrologueParams pp;
+  std::memset(&pp, 0, sizeof pp);
+  pp.nsets = 12;
+  for (int c = 0; c < 3; c++)
+    for (int q = 0; q < 2; q++) {
+      pp.sets[c * 2 + q] = s->setsH[c][q];
+      pp.sets[6 + c * 2 + q] = s->setsE[c][q];
+    }
+  pp.tab = s->tab;
+  pp.tab_total = sp.tfsf ? s->tab_total : 0;
+  pp.planar = s->planar;
+  pp.dx = s->k.dx; pp.dy = s->k.dy; pp.dz = s->k.dz;
+  pp.kx = s->k.k[0]; pp.ky = s->k.k[1]; pp.kz = s->k.k[2];
+  pp.init = s->k.init; pp.c = s->k.c; pp.dt = s->k.dt; pp.mu0 = s->k.mew0; pp.pw_sigma = s->k.sigma;
+  pp.scale_units = s->uniform ? 0.0 : 1.0;
+  pp.src_kind = s->src_kind;
+  pp.src_idx = s->src_idx;
+  pp.src_field = s->planar ? s->E[1] : s->E[2];
+  pp.src_amp_i = (int)s->p.amp_source;  // maxwell.cc:142-143 store them in int members
+  pp.src_omega_i = (int)s->p.omega_source;
+  pp.src_amp = s->p.amp_source;
+  pp.src_omega = s->p.omega_source;
+  pp.src_t0 = s->p.src_t0;
+  pp.src_tw = s->p.src_tw;
+  pp.prec = s->prec;
+  T* pf[6] = {(T*)s->E[0], (T*)s->E[1], (T*)s->E[2], (T*)s->H[0], (T*)s->H[1], (T*)s->H[2]};
+  lx::ProbeParams prb;
+  std::memset(&prb, 0, sizeof prb);
+  prb.nprobes = s->nprobes;
+  prb.Ny = s->Ny;
+  prb.Nzp = s->Nzp;
+  for (int c = 0; c < 6; c++)
+    for (int a = 0; a < 3; a++) prb.ext[c][a] = s->ext[c][a];
+  prb.ijk = s->d_probe_ijk;
+
+  for (int q = 0; q < nsteps; q++) {
+    const int t = s->t;
+    bool mon = (q == nsteps - 1) || (s->p.monitor_every > 0 && (t + 1) % s->p.monitor_every == 0);
+    unsigned snap = 0;
+    for (auto& o : s->outputs)
+      if (o.every > 0 && t % o.every == 0) snap |= o.mask;
+    if (pp.tab_total > 0 || s->src_kind >= 0 || mon) {
+      pp.t = t;
+      pp.max_slot = mon ? s->d_max : nullptr;
+      if (s->csize == 8) CK(lx::launch_prologue<double>(pp, s->stream));
+      else CK(lx::launch_prologue<float>(pp, s->stream));
+      s->n_kernels++;
+    }
+    CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, true, s->stream));
+    sp.max_slot = mon ? s->d_max : nullptr;
+    sp.etotal = (snap & (1u << LX_ETOTAL)) ? (C*)s->etotal : nullptr;
+    CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, false, s->stream));
+    s->n_kernels += 2;
+    if (s->nprobes > 0 && s->probe_rows < s->probe_cap) {
+      prb.row = s->probe_rows++;
+      CK(lx::launch_probes<T>(prb, pf, s->d_probe, s->stream));
+      s->n_kernels++;
+    }
+    s->t++;
+    if (snap) {
+      lx_status st = snapshot(s, t, snap);
+      if (st) return st;
+    }
+  }
+  if (nsteps > 0) {
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, s->d_max, sizeof bits, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    s->n_d2h += sizeof bits;
+    double v;
+    std::memcpy(&v, &bits, sizeof v);
+    s->last_max = v;
+    if (!std::isfinite(v)) {
+      char b[128];
+      std::snprintf(b, sizeof b, "max|E|^2 is not finite after step %d", s->t);
+      return fail(s, LX_ERR_BLOWUP, b);
+    }
+  }
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_step(lx_sim* s, int nsteps) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  if (nsteps < 0) return fail(s, LX_ERR_INVALID, "nsteps must be >= 0");
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->writer_err.empty()) {
+      std::string m = s->writer_err;
+      s->writer_err.clear();
+      return fail(s, LX_ERR_IO, m);
+    }
+  }
+  if (s->prec == LX_PREC_FP64) return run_steps<double, double>(s, nsteps);
+  if (s->prec == LX_PREC_FP32) return run_steps<float, float>(s, nsteps);
+  return run_steps<__half, float>(s, nsteps);
+}
+
+extern "C" LX_API int lx_sim_timestep(const lx_sim* s) { return s ? s->t : -1; }
+
+extern "C" LX_API lx_status lx_sim_max_e2(lx_sim* s, double* out) {
+  if (!s || !out) return fail(s, LX_ERR_INVALID, "null argument");
+  *out = s->last_max;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_set_stream(lx_sim* s, void* stream) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  s->stream = stream ? (cudaStream_t)stream : s->own;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_counters(const lx_sim* s, uint64_t* kernels, uint64_t* h2d, uint64_t* d2h) {
+  if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  if (kernels) *kernels = s->n_kernels;
+  if (h2d) *h2d = s->n_h2d;
+  if (d2h) *d2h = s->n_d2h;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  cudaError_t e = cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocDefault);
+  if (e != cudaSuccess) return fail(nullptr, LX_ERR_OOM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+  return LX_OK;
+}
+
+extern "C" LX_API void lx_host_free(void* ptr) {
+  if (ptr) cudaFreeHost(ptr);
+}

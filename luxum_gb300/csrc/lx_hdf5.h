@@ -1,0 +1,28 @@
+// lx_hdf5.h -- minimal HDF5 writer/reader for the snapshot layout of fileio.cc:60-212.
+#pragma once
+#include <cstdio>
+#include <string>
+#include <vector>
+
+namespace lx {
+
+// Appends one 3-D native-double dataset "t=<step>" per write to a single file.
+class Hdf5Writer {
+ public:
+  ~Hdf5Writer();
+  std::string open(const char* path, const int ext[3]);
+  std::string write(int t, const double* data);
+  std::string close();
+
+ private:
+  struct Entry {
+    std::string name;
+    unsigned long long addr, bytes;
+  };
+  std::FILE* f_ = nullptr;
+  int ext_[3] = {0, 0, 0};
+  unsigned long long eof_ = 0;
+  std::vector<Entry> entries_;
+};
+
+}  // namespace lx

@@ -1,0 +1,118 @@
+// lx_internal.h -- device-side data layout and kernel parameter blocks of the engine.
+//
+// Layout in HBM.  Every field component of one simulation lives in its own array of the
+// common padded shape (Nx, Ny, Nzp), C order (z fastest), Nzp = Nz rounded up to 128 bytes
+// of storage type.  A component only owns the cells of its staggered extent
+// (field.cc:67-77: extent - 1 on every staggered axis); the remaining cells stay zero and
+// are never written.  One shape for all six components lets a single index
+// c = (i*Ny + j)*Nzp + k address every component at cell (i,j,k), so neighbour offsets are
+// the constants 1, Nzp and Ny*Nzp.
+//
+// CPML psi is stored only on the slabs where a 1-D profile is active (c != 0 or kappa != 1):
+// along axis a, indices [0, lo) and [hi0, N) are kept, packed to lo + (N - hi0) entries.
+// Outside them the reference's psi stays exactly 0 (b = 1, c = 0), so dropping it is exact.
+//
+// Difference units.  With uniform spacing (dx = dy = dz, every reference fixture) curls are
+// carried as plain neighbour differences (curl * dx); the 1/dx folds into the coefficients
+// (Db/dx, Cb/dx), the TF/SF increments and psi, which removes two FP64 multiplies per
+// component.  With non-uniform spacing the kernels multiply by 1/d per axis instead.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace lx {
+
+constexpr int kMaxProbes = 64;
+
+// Packed CPML slab along one axis.
+struct Slab {
+  int lo;   // indices [0, lo) are stored as 0..lo-1
+  int hi0;  // indices [hi0, N) are stored as lo..lo+N-hi0-1
+  int n;    // lo + N - hi0 (0: no psi on this axis)
+};
+
+__host__ __device__ inline int slab_index(const Slab& s, int u) {
+  return u < s.lo ? u : (u >= s.hi0 ? u - s.hi0 + s.lo : -1);
+}
+
+// One TF/SF correction set: the two planes (low and high face of the total-field box)
+// that feed one curl part of one component, with the in-plane index ranges of the
+// reference loops (maxwell.cc:512-812) and the layout of its incident-value table.
+struct PatchSet {
+  int active;
+  int axis;        // normal axis of the planes (0 = x, 1 = y, 2 = z)
+  int plane[2];    // cell index along `axis` of the low and high plane
+  int lo[3], hi[3];  // inclusive in-plane ranges (entry `axis` unused)
+  int n[3];        // table extent per axis (1 on `axis` and on axes the wave does not vary along)
+  int stride[3];   // table stride per axis (0 on collapsed axes)
+  int tab;         // offset of the low plane's table in the table buffer
+  int plane_len;   // entries per plane table (high plane at tab + plane_len)
+  // incident-value expression of the table entries
+  double pos_n[2];   // wave position along `axis` of each plane (e.g. p1, p2, p1-0.5, p2+0.5)
+  double off[3];     // in-plane position offsets (0 or 0.5)
+  double sign[2];    // -1 / +1 (curl = curl - v or curl + v)
+  double dir;        // E_?_dir or H_?_dir
+  double neg;        // 1, or -1 for the planar H-curl lines that multiply by (-1) first
+  double dn;         // spacing along `axis` (the reference divides by it)
+  int hcurl;         // 1: also divide by c and mu0 (H-curl lines)
+};
+
+// Parameters of the step prologue: TF/SF tables, point source, monitor reset.
+struct PrologueParams {
+  int nsets;          // 0..12
+  PatchSet sets[12];  // [0,6): E-curl sets for the H update; [6,12): H-curl sets for the E update
+  void* tab;          // table buffer (compute precision; entries evaluated in FP64)
+  int tab_total;      // total entries over all active sets
+  int planar;
+  double dx, dy, dz, kx, ky, kz, init, c, dt, mu0, pw_sigma;
+  double scale_units;  // 1 (curl units) or 0 = scale each entry by its plane spacing (difference units)
+  int t;
+  // point source
+  int src_kind;       // -1 none, 0 hard CW, 1 additive pulse
+  long long src_idx;  // linear index in the padded layout
+  void* src_field;    // Ez (3D) or Ey (planar pulse)
+  int src_amp_i, src_omega_i;
+  double src_amp, src_omega, src_t0, src_tw;
+  int prec;           // storage precision of src_field
+  unsigned long long* max_slot;  // reset to 0 when non-null
+};
+
+// Device pointers and constants of one 3-D or planar simulation, passed by value.
+template <class T, class C>
+struct StepParams {
+  int Nx, Ny, Nz, Nzp;
+  long long sj, si;  // strides of j and i
+  T* E[3];
+  T* H[3];
+  const C* Cbs[3];  // Cb (curl units) or Cb/dx (difference units)
+  C Dbs;            // Db or Db/dx
+  C rd[3];          // 1/dx, 1/dy, 1/dz (non-uniform only)
+  // CPML
+  int pml;
+  Slab slab[3];
+  const C* bE[3];
+  const C* cE[3];
+  const C* rkE[3];
+  const C* bH[3];
+  const C* cH[3];
+  const C* rkH[3];
+  C* psiH[3][2];  // [component][part]
+  C* psiE[3][2];
+  // TF/SF
+  int tfsf;
+  PatchSet setsH[3][2];  // [component][part]
+  PatchSet setsE[3][2];
+  const C* tab;
+  // monitor / |E|^2 snapshot (E kernel)
+  unsigned long long* max_slot;  // atomicMax of the bit pattern of max|E|^2 (non-negative)
+  C* etotal;                     // when non-null, |E|^2 into the Ez-shaped array (3D)
+};
+
+// Probe sampling of one step row.
+struct ProbeParams {
+  int nprobes, row, Ny, Nzp;
+  int ext[6][3];    // staggered extents of the six components (0 for absent ones)
+  const int* ijk;   // device array [nprobes][3]
+};
+
+}  // namespace lx

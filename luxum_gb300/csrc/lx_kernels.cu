@@ -1,0 +1,575 @@
+// lx_kernels.cu -- sm_103a kernels of the Yee time step.
+//
+// One step = prologue (TF/SF incident tables for this step, point source, monitor reset)
+//          -> H kernel (curl E + TF/SF + CPML psi_H + H update, fused)
+//          -> E kernel (curl H + TF/SF + CPML psi_E + E update + max|E|^2, fused)
+// This is the order of every reference driver (e.g. three_dim_pml.cc:158-276): point source,
+// E-curl, TF/SF on the curl, H update with psi, H-curl, TF/SF, E update with psi, |E|^2 max.
+//
+// The reference materialises each curl in a full-grid array and patches it in a separate
+// pass (vfield.cc:196-275, maxwell.cc:512-812).  Here the curl of a cell lives in registers:
+// each thread forms the neighbour differences of its cell, adds the TF/SF increment if the
+// cell lies on a total-field-box plane (one table load), runs the psi recursion only when
+// the cell lies in a CPML slab, and writes the updated component.  Cells outside the slabs
+// and off the planes do 4 FP64 operations per component (3 differences + 1 FMA), which is
+// the bound on GB300, whose FP64 pipe (~0.6 T lane-ops/s) limits before HBM does.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "lx_internal.h"
+#include "lx_kernels.h"
+
+namespace lx {
+
+// ------------------------------------------------------------------ storage access
+
+template <class T, class C>
+__device__ __forceinline__ C ld(const T* p) {
+  return static_cast<C>(*p);
+}
+template <>
+__device__ __forceinline__ float ld<__half, float>(const __half* p) {
+  return __half2float(*p);
+}
+template <class T, class C>
+__device__ __forceinline__ void st(T* p, C v) {
+  *p = static_cast<T>(v);
+}
+template <>
+__device__ __forceinline__ void st<__half, float>(__half* p, float v) {
+  *p = __float2half_rn(v);
+}
+
+__device__ __forceinline__ double fmaC(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmaC(float a, float b, float c) { return fmaf(a, b, c); }
+
+// ------------------------------------------------------------------ TF/SF
+
+// Adds the increments of the planes of `ps` that cell (i,j,k) lies on to d (reference:
+// curl = curl +/- exp(...) * dir / d..., one line of plane_wave_execute per plane).
+template <class C>
+__device__ __forceinline__ void tfsf_apply(const PatchSet& ps, const C* tab, int i, int j, int k, C& d) {
+  if (!ps.active) return;
+  const int u[3] = {i, j, k};
+  const int a = ps.axis;
+  const int n = u[a];
+  const bool h0 = (n == ps.plane[0]);
+  const bool h1 = (n == ps.plane[1]);
+  if (!(h0 || h1)) return;
+  int off = 0;
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    if (b == a) continue;
+    if (u[b] < ps.lo[b] || u[b] > ps.hi[b]) return;
+    off += (u[b] - ps.lo[b]) * ps.stride[b];
+  }
+  if (h0) d = d + tab[ps.tab + off];
+  if (h1) d = d + tab[ps.tab + ps.plane_len + off];
+}
+
+// psi = b*psi + c*curl; returns curl/kappa + psi (reference: three_dim_pml.cc:186-188).
+template <class C>
+__device__ __forceinline__ C pml_term(C d, C* psi, C b, C cc, C rk) {
+  C ps = fmaC(b, *psi, cc * d);
+  *psi = ps;
+  return fmaC(d, rk, ps);
+}
+
+__device__ __forceinline__ long long psi_index(int axis, const Slab& s, int si_, int i, int j, int k, int Ny,
+                                               int Nzp) {
+  if (axis == 0) return ((long long)si_ * Ny + j) * Nzp + k;
+  if (axis == 1) return ((long long)i * s.n + si_) * Nzp + k;
+  return ((long long)i * Ny + j) * s.n + si_;
+}
+
+// ------------------------------------------------------------------ prologue
+
+__device__ double incident_value(const PrologueParams& p, const PatchSet& ps, int plane, int e) {
+  // table entry e of `plane` -> in-plane indices -> wave positions
+  double pos[3];
+  int rem = e;
+#pragma unroll
+  for (int b = 2; b >= 0; --b) {
+    if (b == ps.axis) {
+      pos[b] = ps.pos_n[plane];
+      continue;
+    }
+    const int nb = ps.n[b];
+    const int ib = rem % nb;
+    rem /= nb;
+    pos[b] = (double)(ps.lo[b] + ib) + ps.off[b];
+  }
+  // ((x*dx*kx + y*dy*ky + z*dz*kz) + init*dx) - t*c*dt   (maxwell.cc:289 and siblings;
+  // the planar lines have no y term, maxwell.cc:206)
+  double X;
+  if (p.planar)
+    X = __dadd_rn(__dmul_rn(__dmul_rn(pos[0], p.dx), p.kx), __dmul_rn(__dmul_rn(pos[2], p.dz), p.kz));
+  else
+    X = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(pos[0], p.dx), p.kx), __dmul_rn(__dmul_rn(pos[1], p.dy), p.ky)),
+                  __dmul_rn(__dmul_rn(pos[2], p.dz), p.kz));
+  const double tt = ps.hcurl ? (double)p.t : (double)p.t - 0.5;
+  X = __dsub_rn(__dadd_rn(X, __dmul_rn(p.init, p.dx)), __dmul_rn(__dmul_rn(tt, p.c), p.dt));
+  double v = exp(__ddiv_rn(-__dmul_rn(X, X), p.pw_sigma));
+  v = __dmul_rn(v, ps.neg);
+  v = __dmul_rn(v, ps.dir);
+  v = __ddiv_rn(v, ps.dn);
+  if (ps.hcurl) v = __ddiv_rn(__ddiv_rn(v, p.c), p.mu0);
+  if (p.scale_units == 0.0) v = __dmul_rn(v, ps.dn);  // difference units
+  return ps.sign[plane] < 0 ? -v : v;
+}
+
+template <class C>
+__global__ void prologue_kernel(const PrologueParams p, C* tab_out) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid == 0) {
+    if (p.max_slot) *p.max_slot = 0ull;
+    if (p.src_kind == 0) {
+      // amp_source*sin(omega_source*t*dt), int members (maxwell.h:203,206; three_dim_pml.cc:163)
+      const int wt = (int)((unsigned)p.src_omega_i * (unsigned)p.t);
+      const double v = (double)p.src_amp_i * sin((double)wt * p.dt);
+      if (p.prec == 0) ((double*)p.src_field)[p.src_idx] = v;
+      else if (p.prec == 1) ((float*)p.src_field)[p.src_idx] = (float)v;
+      else ((__half*)p.src_field)[p.src_idx] = __double2half(v);
+    } else if (p.src_kind == 1) {
+      const double u = (p.t - p.src_t0) / p.src_tw;
+      const double v = p.src_amp * exp(-(u * u)) * sin(p.src_omega * p.t * p.dt);
+      if (p.prec == 0) ((double*)p.src_field)[p.src_idx] += v;
+      else if (p.prec == 1) ((float*)p.src_field)[p.src_idx] += (float)v;
+      else {
+        __half* f = (__half*)p.src_field;
+        f[p.src_idx] = __float2half_rn(__half2float(f[p.src_idx]) + (float)v);
+      }
+    }
+  }
+  for (int e = gid; e < p.tab_total; e += gridDim.x * blockDim.x) {
+    int rem = e;
+    for (int s = 0; s < p.nsets; ++s) {
+      const PatchSet& ps = p.sets[s];
+      if (!ps.active) continue;
+      const int len = 2 * ps.plane_len;
+      if (rem < len) {
+        const int plane = rem >= ps.plane_len ? 1 : 0;
+        const double v = incident_value(p, ps, plane, rem - plane * ps.plane_len);
+        tab_out[ps.tab + rem] = (C)v;
+        break;
+      }
+      rem -= len;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ monitor
+
+__device__ __forceinline__ void block_max_atomic(unsigned long long v, unsigned long long* slot) {
+  __shared__ unsigned long long red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int nw = (blockDim.x * blockDim.y + 31) / 32;
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    v = tid < nw ? red[tid] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = w > v ? w : v;
+    }
+    if (tid == 0 && v) atomicMax(slot, v);
+  }
+}
+
+__device__ __forceinline__ unsigned long long e2_bits(double v) { return (unsigned long long)__double_as_longlong(v); }
+__device__ __forceinline__ unsigned long long e2_bits(float v) {
+  return (unsigned long long)__double_as_longlong((double)v);
+}
+
+// ------------------------------------------------------------------ 3-D kernels
+
+// H half-step over cell (i,j,k) for Hx, Hy, Hz (three_dim_pml.cc:176-213, three_dim.cc:101-132).
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) h_kernel_3d(const StepParams<T, C> p) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int i = blockIdx.z;
+  if (k >= p.Nz || j >= p.Ny) return;
+  const long long c = (long long)i * p.si + (long long)j * p.sj + k;
+  const C ex = ld<T, C>(p.E[0] + c), ey = ld<T, C>(p.E[1] + c), ez = ld<T, C>(p.E[2] + c);
+  int sx = -1, sy = -1, sz = -1;
+  if (p.pml) {
+    sx = slab_index(p.slab[0], i);
+    sy = slab_index(p.slab[1], j);
+    sz = slab_index(p.slab[2], k);
+  }
+  // Hx: i < Nx, j < Ny-1, k < Nz-1; part 1 = dEz/dy (y profile), part 2 = dEy/dz (z profile)
+  if (j < p.Ny - 1 && k < p.Nz - 1) {
+    C d1 = ld<T, C>(p.E[2] + c + p.sj) - ez;
+    C d2 = ld<T, C>(p.E[1] + c + 1) - ey;
+    if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
+    if (p.tfsf) {
+      tfsf_apply<C>(p.setsH[0][0], p.tab, i, j, k, d1);
+      tfsf_apply<C>(p.setsH[0][1], p.tab, i, j, k, d2);
+    }
+    if (sy >= 0) d1 = pml_term<C>(d1, p.psiH[0][0] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bH[1][j], p.cH[1][j], p.rkH[1][j]);
+    if (sz >= 0) d2 = pml_term<C>(d2, p.psiH[0][1] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bH[2][k], p.cH[2][k], p.rkH[2][k]);
+    const C h = ld<T, C>(p.H[0] + c);
+    st<T, C>(p.H[0] + c, fmaC(-p.Dbs, d1 - d2, h));
+  }
+  // Hy: i < Nx-1, j < Ny, k < Nz-1; part 1 = dEx/dz (z), part 2 = dEz/dx (x)
+  if (i < p.Nx - 1 && k < p.Nz - 1) {
+    C d1 = ld<T, C>(p.E[0] + c + 1) - ex;
+    C d2 = ld<T, C>(p.E[2] + c + p.si) - ez;
+    if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
+    if (p.tfsf) {
+      tfsf_apply<C>(p.setsH[1][0], p.tab, i, j, k, d1);
+      tfsf_apply<C>(p.setsH[1][1], p.tab, i, j, k, d2);
+    }
+    if (sz >= 0) d1 = pml_term<C>(d1, p.psiH[1][0] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bH[2][k], p.cH[2][k], p.rkH[2][k]);
+    if (sx >= 0) d2 = pml_term<C>(d2, p.psiH[1][1] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bH[0][i], p.cH[0][i], p.rkH[0][i]);
+    const C h = ld<T, C>(p.H[1] + c);
+    st<T, C>(p.H[1] + c, fmaC(-p.Dbs, d1 - d2, h));
+  }
+  // Hz: i < Nx-1, j < Ny-1, k < Nz; part 1 = dEy/dx (x), part 2 = dEx/dy (y)
+  if (i < p.Nx - 1 && j < p.Ny - 1) {
+    C d1 = ld<T, C>(p.E[1] + c + p.si) - ey;
+    C d2 = ld<T, C>(p.E[0] + c + p.sj) - ex;
+    if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
+    if (p.tfsf) {
+      tfsf_apply<C>(p.setsH[2][0], p.tab, i, j, k, d1);
+      tfsf_apply<C>(p.setsH[2][1], p.tab, i, j, k, d2);
+    }
+    if (sx >= 0) d1 = pml_term<C>(d1, p.psiH[2][0] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bH[0][i], p.cH[0][i], p.rkH[0][i]);
+    if (sy >= 0) d2 = pml_term<C>(d2, p.psiH[2][1] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bH[1][j], p.cH[1][j], p.rkH[1][j]);
+    const C h = ld<T, C>(p.H[2] + c);
+    st<T, C>(p.H[2] + c, fmaC(-p.Dbs, d1 - d2, h));
+  }
+}
+
+// E half-step over cell (i,j,k) for Ex, Ey, Ez (three_dim_pml.cc:218-276, three_dim.cc:134-189).
+// Only cells where the reference's H-curl is computed (vfield.cc:241-269: the transverse
+// index in [1, N-2]) change; on the PEC walls the reference adds Cb*0 and psi stays 0.
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int i = blockIdx.z;
+  const bool in = (k < p.Nz && j < p.Ny);
+  unsigned long long mbits = 0ull;
+  if (in) {
+    const long long c = (long long)i * p.si + (long long)j * p.sj + k;
+    const C hx = ld<T, C>(p.H[0] + c), hy = ld<T, C>(p.H[1] + c), hz = ld<T, C>(p.H[2] + c);
+    int sx = -1, sy = -1, sz = -1;
+    if (p.pml) {
+      sx = slab_index(p.slab[0], i);
+      sy = slab_index(p.slab[1], j);
+      sz = slab_index(p.slab[2], k);
+    }
+    const bool ii = (i >= 1 && i < p.Nx - 1), jj = (j >= 1 && j < p.Ny - 1), kk = (k >= 1 && k < p.Nz - 1);
+    const bool mon = (p.max_slot != nullptr || p.etotal != nullptr) && i < p.Nx - 1 && j < p.Ny - 1 && k < p.Nz - 1;
+    C exn = 0, eyn = 0, ezn = 0;
+    // Ex: i < Nx-1, j in [1,Ny-2], k in [1,Nz-2]; part 1 = dHz/dy (y), part 2 = dHy/dz (z)
+    if (i < p.Nx - 1 && jj && kk) {
+      C d1 = hz - ld<T, C>(p.H[2] + c - p.sj);
+      C d2 = hy - ld<T, C>(p.H[1] + c - 1);
+      if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
+      if (p.tfsf) {
+        tfsf_apply<C>(p.setsE[0][0], p.tab, i, j, k, d1);
+        tfsf_apply<C>(p.setsE[0][1], p.tab, i, j, k, d2);
+      }
+      if (sy >= 0) d1 = pml_term<C>(d1, p.psiE[0][0] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bE[1][j], p.cE[1][j], p.rkE[1][j]);
+      if (sz >= 0) d2 = pml_term<C>(d2, p.psiE[0][1] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
+      exn = fmaC(p.Cbs[0][c], d1 - d2, ld<T, C>(p.E[0] + c));
+      st<T, C>(p.E[0] + c, exn);
+    } else if (mon) {
+      exn = ld<T, C>(p.E[0] + c);
+    }
+    // Ey: i in [1,Nx-2], j < Ny-1, k in [1,Nz-2]; part 1 = dHx/dz (z), part 2 = dHz/dx (x)
+    if (ii && j < p.Ny - 1 && kk) {
+      C d1 = hx - ld<T, C>(p.H[0] + c - 1);
+      C d2 = hz - ld<T, C>(p.H[2] + c - p.si);
+      if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
+      if (p.tfsf) {
+        tfsf_apply<C>(p.setsE[1][0], p.tab, i, j, k, d1);
+        tfsf_apply<C>(p.setsE[1][1], p.tab, i, j, k, d2);
+      }
+      if (sz >= 0) d1 = pml_term<C>(d1, p.psiE[1][0] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
+      if (sx >= 0) d2 = pml_term<C>(d2, p.psiE[1][1] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
+      eyn = fmaC(p.Cbs[1][c], d1 - d2, ld<T, C>(p.E[1] + c));
+      st<T, C>(p.E[1] + c, eyn);
+    } else if (mon) {
+      eyn = ld<T, C>(p.E[1] + c);
+    }
+    // Ez: i in [1,Nx-2], j in [1,Ny-2], k < Nz-1; part 1 = dHy/dx (x), part 2 = dHx/dy (y)
+    if (ii && jj && k < p.Nz - 1) {
+      C d1 = hy - ld<T, C>(p.H[1] + c - p.si);
+      C d2 = hx - ld<T, C>(p.H[0] + c - p.sj);
+      if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
+      if (p.tfsf) {
+        tfsf_apply<C>(p.setsE[2][0], p.tab, i, j, k, d1);
+        tfsf_apply<C>(p.setsE[2][1], p.tab, i, j, k, d2);
+      }
+      if (sx >= 0) d1 = pml_term<C>(d1, p.psiE[2][0] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
+      if (sy >= 0) d2 = pml_term<C>(d2, p.psiE[2][1] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bE[1][j], p.cE[1][j], p.rkE[1][j]);
+      ezn = fmaC(p.Cbs[2][c], d1 - d2, ld<T, C>(p.E[2] + c));
+      st<T, C>(p.E[2] + c, ezn);
+    } else if (mon) {
+      ezn = ld<T, C>(p.E[2] + c);
+    }
+    if (mon) {
+      // Etotal = Ez*Ez + Ey*Ey + Ex*Ex (three_dim_pml.cc:270), same association order
+      C e2 = fmaC(exn, exn, fmaC(eyn, eyn, ezn * ezn));
+      if (p.etotal) p.etotal[c] = e2;
+      mbits = e2_bits(e2);
+    }
+  }
+  if (p.max_slot) block_max_atomic(mbits, p.max_slot);
+}
+
+// ------------------------------------------------------------------ planar kernels
+
+// Planar H half-step (x-z plane, Ny = 1): Hx and Hz (two_dim_pml.cc:144-162, two_dim.cc:95-111).
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int i = blockIdx.y * 8 + threadIdx.y;
+  if (k >= p.Nz || i >= p.Nx) return;
+  const long long c = (long long)i * p.si + k;
+  const C ey = ld<T, C>(p.E[1] + c);
+  // Hx: k < Nz-1; Hx -= Db*(-curl2/kappa - psi2), curl2 = dEy/dz (z profile)
+  if (k < p.Nz - 1) {
+    C d2 = ld<T, C>(p.E[1] + c + 1) - ey;
+    if (!UNI) d2 *= p.rd[2];
+    if (p.tfsf) tfsf_apply<C>(p.setsH[0][1], p.tab, i, 0, k, d2);
+    if (p.pml) {
+      const int sz = slab_index(p.slab[2], k);
+      if (sz >= 0) d2 = pml_term<C>(d2, p.psiH[0][1] + (long long)i * p.slab[2].n + sz, p.bH[2][k], p.cH[2][k], p.rkH[2][k]);
+    }
+    st<T, C>(p.H[0] + c, fmaC(p.Dbs, d2, ld<T, C>(p.H[0] + c)));
+  }
+  // Hz: i < Nx-1; Hz -= Db*(curl1/kappa + psi1), curl1 = dEy/dx (x profile)
+  if (i < p.Nx - 1) {
+    C d1 = ld<T, C>(p.E[1] + c + p.si) - ey;
+    if (!UNI) d1 *= p.rd[0];
+    if (p.tfsf) tfsf_apply<C>(p.setsH[2][0], p.tab, i, 0, k, d1);
+    if (p.pml) {
+      const int sx = slab_index(p.slab[0], i);
+      if (sx >= 0) d1 = pml_term<C>(d1, p.psiH[2][0] + (long long)sx * p.Nzp + k, p.bH[0][i], p.cH[0][i], p.rkH[0][i]);
+    }
+    st<T, C>(p.H[2] + c, fmaC(-p.Dbs, d1, ld<T, C>(p.H[2] + c)));
+  }
+}
+
+// Planar E half-step: Ey (two_dim_pml.cc:164-181, two_dim.cc:113-128).  The reference loop
+// covers i < Nx-1, k < Nz-1, but its H-curl is only computed for i, k in [1, N-2]
+// (vfield.cc:376-381), so the other cells add Cb*0 and are skipped here.
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int i = blockIdx.y * 8 + threadIdx.y;
+  unsigned long long mbits = 0ull;
+  if (k < p.Nz && i < p.Nx) {
+    const long long c = (long long)i * p.si + k;
+    C eyn;
+    if (i >= 1 && i < p.Nx - 1 && k >= 1 && k < p.Nz - 1) {
+      C d1 = ld<T, C>(p.H[0] + c) - ld<T, C>(p.H[0] + c - 1);     // dHx/dz (z profile)
+      C d2 = ld<T, C>(p.H[2] + c) - ld<T, C>(p.H[2] + c - p.si);  // dHz/dx (x profile)
+      if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
+      if (p.tfsf) {
+        tfsf_apply<C>(p.setsE[1][0], p.tab, i, 0, k, d1);
+        tfsf_apply<C>(p.setsE[1][1], p.tab, i, 0, k, d2);
+      }
+      if (p.pml) {
+        const int sz = slab_index(p.slab[2], k), sx = slab_index(p.slab[0], i);
+        if (sz >= 0) d1 = pml_term<C>(d1, p.psiE[1][0] + (long long)i * p.slab[2].n + sz, p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
+        if (sx >= 0) d2 = pml_term<C>(d2, p.psiE[1][1] + (long long)sx * p.Nzp + k, p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
+      }
+      eyn = fmaC(p.Cbs[1][c], d1 - d2, ld<T, C>(p.E[1] + c));
+      st<T, C>(p.E[1] + c, eyn);
+    } else {
+      eyn = ld<T, C>(p.E[1] + c);
+    }
+    // local_max = max(Ey*Ey) over the whole Ey array (two_dim_pml.cc:181)
+    if (p.max_slot) mbits = e2_bits(eyn * eyn);
+  }
+  if (p.max_slot) block_max_atomic(mbits, p.max_slot);
+}
+
+// ------------------------------------------------------------------ data movement
+
+// padded (Nx,Ny,Nzp) storage -> dense double array of extent (n0,n1,n2)
+template <class T>
+__global__ void gather_kernel(const T* __restrict__ src, double* __restrict__ dst, int n0, int n1, int n2, int Ny,
+                              int Nzp) {
+  const long long total = (long long)n0 * n1 * n2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(q % n2);
+    const long long r = q / n2;
+    const int j = (int)(r % n1);
+    const int i = (int)(r / n1);
+    dst[q] = (double)src[((long long)i * Ny + j) * Nzp + k];
+  }
+}
+template <>
+__global__ void gather_kernel<__half>(const __half* __restrict__ src, double* __restrict__ dst, int n0, int n1, int n2,
+                                      int Ny, int Nzp) {
+  const long long total = (long long)n0 * n1 * n2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(q % n2);
+    const long long r = q / n2;
+    const int j = (int)(r % n1);
+    const int i = (int)(r / n1);
+    dst[q] = (double)__half2float(src[((long long)i * Ny + j) * Nzp + k]);
+  }
+}
+
+// dense double array -> padded storage (optionally Cb-style transform)
+// mode 0: dst = v; mode 1: dst = v * a (Cb -> Cb/dx); mode 2: Cb = dt/(eps0*(1+F*scale)) * a
+template <class T>
+__global__ void scatter_kernel(const double* __restrict__ src, T* __restrict__ dst, int n0, int n1, int n2, int Ny,
+                               int Nzp, int mode, double a, double dt, double eps0, double scale) {
+  const long long total = (long long)n0 * n1 * n2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(q % n2);
+    const long long r = q / n2;
+    const int j = (int)(r % n1);
+    const int i = (int)(r / n1);
+    double v = src[q];
+    if (mode == 2) {
+      // epsilon0*(1+F*1000000) then dt/that (three_dim_pml.cc:122-128), no contraction
+      const double e = __dmul_rn(eps0, __dadd_rn(1.0, __dmul_rn(v, scale)));
+      v = __ddiv_rn(dt, e);
+    }
+    if (mode >= 1) v = __dmul_rn(v, a);
+    const long long o = ((long long)i * Ny + j) * Nzp + k;
+    if constexpr (sizeof(T) == 2) dst[o] = __double2half(v);
+    else dst[o] = (T)v;
+  }
+}
+
+// Cb = dt/(eps0*eps_r) * a over the box [lo, hi) clipped to the extent
+template <class C>
+__global__ void eps_box_kernel(C* dst, int n0, int n1, int n2, int Ny, int Nzp, int lo0, int lo1, int lo2, int hi0,
+                               int hi1, int hi2, double val) {
+  const int a0 = max(lo0, 0), a1 = max(lo1, 0), a2 = max(lo2, 0);
+  const int b0 = min(hi0, n0), b1 = min(hi1, n1), b2 = min(hi2, n2);
+  if (a0 >= b0 || a1 >= b1 || a2 >= b2) return;
+  const long long w0 = b0 - a0, w1 = b1 - a1, w2 = b2 - a2;
+  const long long total = w0 * w1 * w2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+    const int k = a2 + (int)(q % w2);
+    const long long r = q / w2;
+    const int j = a1 + (int)(r % w1);
+    const int i = a0 + (int)(r / w1);
+    dst[((long long)i * Ny + j) * Nzp + k] = (C)val;
+  }
+}
+
+template <class T>
+__global__ void probe_kernel(const ProbeParams pp, const T* f0, const T* f1, const T* f2, const T* f3, const T* f4,
+                             const T* f5, double* out) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= pp.nprobes * 6) return;
+  const int probe = q / 6, comp = q % 6;
+  const T* f[6] = {f0, f1, f2, f3, f4, f5};
+  const int i = pp.ijk[3 * probe], j = pp.ijk[3 * probe + 1], k = pp.ijk[3 * probe + 2];
+  double v = 0.0;
+  if (f[comp] && i >= 0 && j >= 0 && k >= 0 && i < pp.ext[comp][0] && j < pp.ext[comp][1] && k < pp.ext[comp][2]) {
+    const T* src = f[comp] + ((long long)i * pp.Ny + j) * pp.Nzp + k;
+    if constexpr (sizeof(T) == 2) v = (double)__half2float(*src);
+    else v = (double)*src;
+  }
+  out[(long long)pp.row * pp.nprobes * 6 + q] = v;
+}
+
+// ------------------------------------------------------------------ launchers
+
+static inline unsigned grid1d(long long n, int bs) {
+  long long g = (n + bs - 1) / bs;
+  if (g > 152LL * 64) g = 152LL * 64;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+template <class C>
+cudaError_t launch_prologue(const PrologueParams& p, cudaStream_t s) {
+  const int bs = 256;
+  prologue_kernel<C><<<grid1d(p.tab_total > 0 ? p.tab_total : 1, bs), bs, 0, s>>>(p, (C*)p.tab);
+  return cudaGetLastError();
+}
+
+template <class T, class C>
+cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bool h_half, cudaStream_t s) {
+  dim3 block(32, 8);
+  if (planar) {
+    dim3 grid((p.Nz + 31) / 32, (p.Nx + 7) / 8, 1);
+    if (h_half) {
+      if (uniform) h_kernel_2d<T, C, true><<<grid, block, 0, s>>>(p);
+      else h_kernel_2d<T, C, false><<<grid, block, 0, s>>>(p);
+    } else {
+      if (uniform) e_kernel_2d<T, C, true><<<grid, block, 0, s>>>(p);
+      else e_kernel_2d<T, C, false><<<grid, block, 0, s>>>(p);
+    }
+  } else {
+    dim3 grid((p.Nz + 31) / 32, (p.Ny + 7) / 8, p.Nx);
+    if (h_half) {
+      if (uniform) h_kernel_3d<T, C, true><<<grid, block, 0, s>>>(p);
+      else h_kernel_3d<T, C, false><<<grid, block, 0, s>>>(p);
+    } else {
+      if (uniform) e_kernel_3d<T, C, true><<<grid, block, 0, s>>>(p);
+      else e_kernel_3d<T, C, false><<<grid, block, 0, s>>>(p);
+    }
+  }
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_gather(const T* src, double* dst, const int ext[3], int Ny, int Nzp, cudaStream_t s) {
+  const long long n = (long long)ext[0] * ext[1] * ext[2];
+  if (n == 0) return cudaSuccess;
+  gather_kernel<T><<<grid1d(n, 256), 256, 0, s>>>(src, dst, ext[0], ext[1], ext[2], Ny, Nzp);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_scatter(const double* src, T* dst, const int ext[3], int Ny, int Nzp, int mode, double a, double dt,
+                           double eps0, double scale, cudaStream_t s) {
+  const long long n = (long long)ext[0] * ext[1] * ext[2];
+  if (n == 0) return cudaSuccess;
+  scatter_kernel<T><<<grid1d(n, 256), 256, 0, s>>>(src, dst, ext[0], ext[1], ext[2], Ny, Nzp, mode, a, dt, eps0, scale);
+  return cudaGetLastError();
+}
+
+template <class C>
+cudaError_t launch_eps_box(C* dst, const int ext[3], int Ny, int Nzp, const int lo[3], const int hi[3], double val,
+                           cudaStream_t s) {
+  eps_box_kernel<C><<<152 * 4, 256, 0, s>>>(dst, ext[0], ext[1], ext[2], Ny, Nzp, lo[0], lo[1], lo[2], hi[0], hi[1],
+                                            hi[2], val);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_probes(const ProbeParams& pp, T* const f[6], double* out, cudaStream_t s) {
+  const int n = pp.nprobes * 6;
+  probe_kernel<T><<<(n + 127) / 128, 128, 0, s>>>(pp, f[0], f[1], f[2], f[3], f[4], f[5], out);
+  return cudaGetLastError();
+}
+
+#define LX_INST(T, C)                                                                                                  \
+  template cudaError_t launch_step<T, C>(const StepParams<T, C>&, bool, bool, bool, cudaStream_t);                   \
+  template cudaError_t launch_gather<T>(const T*, double*, const int[3], int, int, cudaStream_t);                     \
+  template cudaError_t launch_scatter<T>(const double*, T*, const int[3], int, int, int, double, double, double,      \
+                                         double, cudaStream_t);                                                        \
+  template cudaError_t launch_probes<T>(const ProbeParams&, T* const[6], double*, cudaStream_t);
+LX_INST(double, double)
+LX_INST(float, float)
+LX_INST(__half, float)
+template cudaError_t launch_prologue<double>(const PrologueParams&, cudaStream_t);
+template cudaError_t launch_prologue<float>(const PrologueParams&, cudaStream_t);
+template cudaError_t launch_eps_box<double>(double*, const int[3], int, int, const int[3], const int[3], double,
+                                            cudaStream_t);
+template cudaError_t launch_eps_box<float>(float*, const int[3], int, int, const int[3], const int[3], double,
+                                           cudaStream_t);
+
+}  // namespace lx

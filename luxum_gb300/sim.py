@@ -1,0 +1,170 @@
+"""Python face of the engine: parameters, simulation handles, numpy views of the fields.
+
+Mirrors the reference's objects: `params(...)`/`read_yaml(path)` stand for class reader
+(reader.h:50-174, reader.cc:68-162), `Sim` for the grid/vfield/maxwell trio a driver builds
+(grid.cc:58-95, maxwell.cc:60-148) and its time loop (maxwell.cc:157-174).  Field arrays
+come back in the reference's staggered extents (field.cc:58-77), C order.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import LuxumError, Params
+
+
+def params(**kw) -> Params:
+    """lx_params with the reference defaults, then `kw` applied (names as in reader.h)."""
+    p = Params()
+    _ffi.lib().lx_params_init(C.byref(p))
+    names = {n for n, _ in Params._fields_}
+    for k, v in kw.items():
+        if k not in names:
+            raise KeyError(f"unknown parameter {k!r}")
+        setattr(p, k, v)
+    return p
+
+
+def read_yaml(path: str) -> Params:
+    """Parses a Luxum parameters.yaml (reader::readYAML + checkData)."""
+    p = Params()
+    st = _ffi.lib().lx_params_from_yaml(str(path).encode(), C.byref(p))
+    if st:
+        raise LuxumError(st, _ffi.lib().lx_last_error(None).decode())
+    return p
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Sim:
+    """One simulation on the current GPU (an lx_sim handle)."""
+
+    def __init__(self, p: Params | dict):
+        if isinstance(p, dict):
+            p = params(**p)
+        self.lib = _ffi.lib()
+        self.p = p
+        h = C.c_void_p()
+        st = self.lib.lx_sim_create(C.byref(p), C.byref(h))
+        if st:
+            raise LuxumError(st, self.lib.lx_last_error(None).decode())
+        self.h = h
+        self._cb = None
+
+    # -- lifecycle
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.lx_sim_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int) -> None:
+        if st:
+            raise LuxumError(st, self.lib.lx_last_error(self.h).decode())
+
+    # -- queries
+    def shape(self, comp: int) -> tuple[int, int, int]:
+        s = (C.c_int * 3)()
+        self._check(self.lib.lx_sim_field_shape(self.h, comp, s))
+        return (s[0], s[1], s[2])
+
+    @property
+    def t(self) -> int:
+        return self.lib.lx_sim_timestep(self.h)
+
+    def max_e2(self) -> float:
+        v = C.c_double()
+        self._check(self.lib.lx_sim_max_e2(self.h, C.byref(v)))
+        return v.value
+
+    def counters(self) -> tuple[int, int, int]:
+        k, a, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._check(self.lib.lx_sim_counters(self.h, C.byref(k), C.byref(a), C.byref(b)))
+        return k.value, a.value, b.value
+
+    # -- fields
+    def field(self, comp: int) -> np.ndarray:
+        shp = self.shape(comp)
+        out = np.empty(shp, dtype=np.float64)
+        self._check(self.lib.lx_sim_read_field(self.h, comp, _dptr(out), out.size))
+        return out
+
+    def set_field(self, comp: int, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.shape != self.shape(comp):
+            raise ValueError(f"shape {a.shape} != {self.shape(comp)}")
+        self._check(self.lib.lx_sim_write_field(self.h, comp, _dptr(a), a.size))
+
+    def set_cb(self, comp: int, cb: np.ndarray) -> None:
+        cb = np.ascontiguousarray(cb, dtype=np.float64)
+        self._check(self.lib.lx_sim_set_cb(self.h, comp, _dptr(cb), cb.size))
+
+    def set_material(self, comp: int, F: np.ndarray, scale: float = 1e6) -> None:
+        F = np.ascontiguousarray(F, dtype=np.float64)
+        self._check(self.lib.lx_sim_set_material(self.h, comp, _dptr(F), F.size, scale))
+
+    def set_eps_box(self, lo, hi, eps_r: float) -> None:
+        self._check(self.lib.lx_sim_set_eps_box(self.h, (C.c_int * 3)(*lo), (C.c_int * 3)(*hi), eps_r))
+
+    # -- stepping
+    def step(self, n: int = 1) -> None:
+        self._check(self.lib.lx_sim_step(self.h, n))
+
+    def sync(self) -> None:
+        self._check(self.lib.lx_sim_sync(self.h))
+
+    def reset(self) -> None:
+        self._check(self.lib.lx_sim_reset(self.h))
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        self._check(self.lib.lx_sim_set_stream(self.h, C.c_void_p(stream_handle or 0)))
+
+    # -- probes / snapshots
+    def set_probes(self, ijk, capacity: int) -> None:
+        a = np.ascontiguousarray(np.asarray(ijk, dtype=np.int32).reshape(-1, 3))
+        self._check(self.lib.lx_sim_set_probes(self.h, a.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], capacity))
+        self._nprobes = a.shape[0]
+        self._probe_cap = capacity
+
+    def probes(self) -> np.ndarray:
+        n = getattr(self, "_nprobes", 0)
+        cap = getattr(self, "_probe_cap", 0)
+        out = np.zeros((max(cap, 1), max(n, 1), 6), dtype=np.float64)
+        rows = C.c_int()
+        self._check(self.lib.lx_sim_read_probes(self.h, _dptr(out), out.size, C.byref(rows)))
+        return out[: rows.value, :n]
+
+    def set_snapshots(self, every: int, mask: int, fn: Callable[[int, int, np.ndarray], None] | None) -> None:
+        """fn(t, comp, array) is called from the handle's writer thread with a copy."""
+        if fn is None or every == 0:
+            self._cb = None
+            self._check(self.lib.lx_sim_set_snapshots(self.h, 0, 0, _ffi.SNAPSHOT_FN(), None))
+            return
+
+        def trampoline(user, t, comp, data, shape):
+            shp = (shape[0], shape[1], shape[2])
+            n = shp[0] * shp[1] * shp[2]
+            arr = np.ctypeslib.as_array(data, shape=(n,)).reshape(shp).copy()
+            fn(t, comp, arr)
+
+        self._cb = _ffi.SNAPSHOT_FN(trampoline)
+        self._check(self.lib.lx_sim_set_snapshots(self.h, every, mask, self._cb, None))
+
+    def set_hdf5_output(self, every: int, comp: int, path: str) -> None:
+        self._check(self.lib.lx_sim_set_hdf5_output(self.h, every, comp, str(path).encode()))

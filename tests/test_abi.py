@@ -1,0 +1,122 @@
+"""The C ABI (include/luxum.h) on the CPU: exports, parameter defaults, validation, YAML.
+
+No compute call is made here: lx_sim_create validates its parameters before touching the
+GPU, so every rejection path runs without one.
+"""
+import ctypes as C
+import math
+import pathlib
+import re
+
+import pytest
+
+import cases
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "luxum.h").read_text()
+    return sorted(set(re.findall(r"^LX_API\s+[\w\s\*]*?\b(lx_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_api():
+    names = declared_symbols()
+    assert "lx_sim_create" in names and "lx_sim_step" in names and len(names) >= 20
+
+
+def test_library_exports_every_declared_symbol(engine):
+    for name in declared_symbols():
+        assert hasattr(engine, name), name
+
+
+def test_params_struct_layout_matches_c(oracle_lib):
+    from luxum_gb300._ffi import Params
+
+    assert C.sizeof(Params) == oracle_lib.ox_params_size()
+
+
+def test_param_defaults(engine):
+    from luxum_gb300 import params
+
+    p = params()
+    assert p.pw_sigma == pow(10, -4) / 0.5  # maxwell.cc:71
+    assert (p.npX, p.npY, p.precision, p.cpml_mode, p.source_kind) == (1, 1, 0, 0, 0)
+
+
+BAD = {
+    # reader::checkData (reader.cc:141-162)
+    "x_not_divisible": dict(isPlanar=0, Nx=33, Ny=30, Nz=30, npX=2),
+    "planar_Ny": dict(isPlanar=1, Nx=30, Ny=3, Nz=30),
+    "planar_npY": dict(isPlanar=1, Nx=30, Ny=1, Nz=30, npY=3),
+    # index ranges the reference reads out of bounds
+    "box_touches_wall": dict(isPlanar=0, Nx=30, Ny=30, Nz=30, **cases.pw((1, 0, 0), (0, 0, 1), ((0, 20), (5, 20), (5, 20)))),
+    "box_past_wall": dict(isPlanar=1, Nx=30, Ny=1, Nz=30, **cases.pw((1, 0, 0), (0, 1, 0), ((5, 29), (0, 0), (5, 20)))),
+    "k_parallel_E": dict(isPlanar=0, Nx=30, Ny=30, Nz=30, **cases.pw((1, 0, 0), (1, 0, 0), ((5, 20), (5, 20), (5, 20)))),
+    "pml_one_cell": dict(isPlanar=0, Nx=30, Ny=30, Nz=30, **cases.pml(1)),
+    "pml_fractional_m": dict(isPlanar=0, Nx=30, Ny=30, Nz=30, **cases.pml(5, m=2.5)),
+    "source_z_outside": dict(isPlanar=0, Nx=30, Ny=30, Nz=30, usePS=1, Nx_source=3, Ny_source=3, Nz_source=29),
+    "tiny_grid": dict(isPlanar=0, Nx=2, Ny=30, Nz=30),
+}
+
+
+@pytest.mark.parametrize("name", sorted(BAD))
+def test_invalid_parameters_rejected_like_oracle(name, engine, oracle_lib):
+    from oracle.oracle import OracleError, OracleSim
+
+    p = cases.make(**BAD[name])
+    h = C.c_void_p()
+    st = engine.lx_sim_create(C.byref(p), C.byref(h))
+    assert st == 1, (name, st, engine.lx_last_error(None))
+    assert engine.lx_last_error(None)
+    with pytest.raises(OracleError) as ei:
+        OracleSim(p)
+    assert ei.value.status == 1
+
+
+def test_planar_point_source_unsupported(engine):
+    """The reference writes E->Vz in planar mode, which does not exist (vfield.cc:69-71)."""
+    p = cases.make(isPlanar=1, Nx=30, Ny=1, Nz=30, usePS=1, Nx_source=5, Nz_source=5)
+    h = C.c_void_p()
+    assert engine.lx_sim_create(C.byref(p), C.byref(h)) == 2
+    assert b"Vz" in engine.lx_last_error(None)
+
+
+def test_yaml_fixture_2d(engine):
+    from luxum_gb300 import read_yaml
+
+    p = read_yaml(GOLDEN / "params_2d.yaml")
+    assert (p.isPlanar, p.Nx, p.Ny, p.Nz) == (1, 130, 1, 130)
+    assert p.dx == 0.001 and p.dy == 0 and p.S == 0.5 and p.num_timesteps == 300
+    assert (p.npX, p.npY, p.n_threads) == (2, 1, 4)
+    assert p.usePW == 1 and p.usePS == 0 and p.kx_pw == 1 and p.Ey_pw == 1 and p.off_pw == 40
+    assert (p.x1_pw, p.x2_pw, p.z1_pw, p.z2_pw) == (25, 104, 25, 104)
+    assert p.usePML == 1 and p.d_pml == 0.02 and p.kappa == 5 and p.a_max == 0.05
+
+
+def test_yaml_fixture_3d_engine_options(engine):
+    from luxum_gb300 import read_yaml
+
+    p = read_yaml(GOLDEN / "params_3d.yaml")
+    assert (p.isPlanar, p.Nx, p.Ny, p.Nz) == (0, 66, 66, 66)
+    assert math.isclose(p.kx_pw, 1 / math.sqrt(3), rel_tol=1e-12)
+    assert p.precision == 1 and p.cpml_mode == 1 and p.monitor_every == 10
+
+
+@pytest.mark.parametrize("mutation, status", [
+    (lambda s: s.replace('"X Length": 130,', ''), 6),           # missing key
+    (lambda s: s.replace('"X Length": 130', '"X Length": 1.5e2'), 6),  # not an integer
+    (lambda s: s.replace('"usePW": true', '"usePW": maybe'), 6),     # not a boolean
+    (lambda s: s.replace('"X Number of Procs": 2', '"X Number of Procs": 3'), 1),  # checkData
+    (lambda s: s[: s.index("{   # absorbing layer")], 6),          # four documents only
+])
+def test_yaml_errors(engine, tmp_path, mutation, status):
+    from luxum_gb300 import LuxumError, read_yaml
+
+    src = (GOLDEN / "params_2d.yaml").read_text(encoding="utf-8")
+    bad = tmp_path / "parameters.yaml"
+    bad.write_text(mutation(src), encoding="utf-8")
+    with pytest.raises(LuxumError) as ei:
+        read_yaml(bad)
+    assert ei.value.status == status
