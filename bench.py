@@ -1,0 +1,388 @@
+#!/usr/bin/env python3
+"""Headline benchmark of the GB300 FDTD engine.
+
+Workload (one bench step = one whole simulation): 3-D Yee grid 256^3, FP64, 1000 time
+steps; x-directed Gaussian plane wave (pulse 1/e half-width 14.1 cells = 28 steps) injected
+through a TF/SF box [32,223]^3 that sits 16 cells inside a 16-cell CPML (m=3, kappa 15);
+centred 48^3 dielectric cube eps_r = 6; snapshots of Ex..Hz every 250 steps; 8 seeded
+point probes recording all six components every step.  Synthetic inputs of the stated
+shapes (the reference ships no dataset).
+
+value : Gcell-updates/s with the material already resident on the GPU (fields reset on
+        the device, snapshots staged to pinned host memory as part of the workload).
+e2e   : the same through the public API from host buffers: each step uploads the three
+        material arrays from pinned memory and reads back every snapshot and the probe
+        series.
+roofline: the dominant kernel's algorithmic bytes per launch / its mean CUDA-event time.
+cpu_baseline / --impl reference: the oracle (CPU restatement of the reference's loops,
+        OpenMP like the reference) on the host cores, on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-updates/s & HBM GB/s vs peak, FP32 vs FP64 at stated err; p50/p99 latency"
+UNIT = "Gcell-updates/s"
+N = 256
+STEPS = 1000
+SNAP_EVERY = 250
+CPML = 16
+BOX = (32, 223)
+CUBE = (104, 152)
+
+
+def workload_params(precision: int = 0):
+    from luxum_gb300 import params
+
+    return params(isPlanar=0, Nx=N, Ny=N, Nz=N, dx=1e-3, dy=1e-3, dz=1e-3, S=0.5, num_timesteps=STEPS,
+                  usePW=1, kx_pw=1.0, ky_pw=0.0, kz_pw=0.0, Ex_pw=0.0, Ey_pw=0.0, Ez_pw=1.0, off_pw=24.0,
+                  x1_pw=BOX[0], x2_pw=BOX[1], y1_pw=BOX[0], y2_pw=BOX[1], z1_pw=BOX[0], z2_pw=BOX[1],
+                  usePML=1, d_pml=CPML * 1e-3, sigma=0.65, sigma_m=3.0, kappa=15.0, a_max=0.0, a_m=1.0,
+                  precision=precision, n_threads=os.cpu_count() or 1)
+
+
+def probe_points():
+    rng = np.random.default_rng(2026)
+    return rng.integers(BOX[0], BOX[1] + 1, size=(8, 3)).astype(np.int32)
+
+
+def material(shape):
+    """F of the reference's material files: Cb = dt/(eps0*(1+F*1e6)) gives eps_r = 6 in the cube."""
+    F = np.zeros(shape)
+    a, b = CUBE
+    F[a:b, a:b, a:b] = (6.0 - 1.0) / 1e6
+    return F
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(self.rows), "reasons": reasons}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def fp64_peak_tflops(torch) -> float:
+    """cuBLAS DGEMM 8192^3 (best of 3): the measured FP64 roof of this GPU."""
+    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    b = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2 * 8192 ** 3 / (best * 1e-3) / 1e12
+
+
+def kernel_model(sim, p):
+    """Algorithmic bytes and FP64 flops per launch of the H and E kernels.
+
+    Bytes: every array a kernel must touch, once: H kernel reads E (3) and H (3) and writes
+    H (3); E kernel reads H (3), E (3), Cb (3) and writes E (3); each stored psi entry is
+    read and written once.  Flops per component: 3 differences + 1 FMA (5 flops); per psi
+    term: psi = b*psi + c*d and d/kappa + psi (5 flops).
+    """
+    el = 8 if p.precision == 0 else (4 if p.precision == 1 else 2)
+    cel = 8 if p.precision == 0 else 4
+    cells = N ** 3
+    slab = 2 * CPML  # slab depth per axis with the 16-cell CPML
+    psi_axis = slab * N * N
+    psi_h = 2 * 3 * psi_axis  # two H components per axis x three axes
+    psi_e = 2 * 3 * psi_axis
+    h_bytes = cells * 9 * el + psi_h * 2 * cel
+    e_bytes = cells * 9 * el + cells * 3 * cel + psi_e * 2 * cel
+    h_flops = cells * 15 + psi_h * 5
+    e_flops = cells * 15 + psi_e * 5
+    return {"h_update": (h_bytes, h_flops), "e_update": (e_bytes, e_flops)}
+
+
+def run_cpu_sample(steps: int, threads: int):
+    from oracle.oracle import OracleSim
+
+    p = workload_params(0)
+    o = OracleSim(p, threads=threads)
+    for c in range(3):
+        o.set_material(c, material(o.shape(c)), 1e6)
+    o.step(1)  # first touch of the arrays
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return N ** 3 * steps / dt / 1e9, dt
+
+
+def dist_setup(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if n_gpus > 1 else "gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def bench_reference(args):
+    """--impl reference: the reference's CPU path (the oracle port) on all host threads."""
+    rank, world, local, pg = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample_steps
+    for _ in range(args.warmup):
+        run_cpu_sample(max(1, sample // 4), threads)
+    vals = []
+    t_all = 0.0
+    for _ in range(args.steps):
+        v, dt = run_cpu_sample(sample, threads)
+        vals.append(v)
+        t_all += dt
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(f"each step: {sample} time steps of the 1000-step run"),
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{sample} time steps of the 256^3 workload per bench step "
+                                       f"({N ** 3 * sample:.3g} cell-updates); the reference needs blitz++, "
+                                       "yaml-cpp 0.3, MPI and HDF5 and is not buildable here, so its loops run "
+                                       "as the oracle restatement (same loop nests, OpenMP, FP64)"}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(extra: str = ""):
+    d = {"workload": f"3D Yee {N}^3 FP64, {STEPS} steps, CPML {CPML} (m=3, kappa 15), TF/SF x-wave box "
+                     f"[{BOX[0]},{BOX[1]}]^3, eps_r 6 cube [{CUBE[0]},{CUBE[1]})^3, Ex..Hz snapshots every "
+                     f"{SNAP_EVERY} steps, 8 probes x 6 components every step",
+         "grid": [N, N, N], "time_steps_per_bench_step": STEPS, "cell_updates_per_bench_step": N ** 3 * STEPS,
+         "l2": "no flush: resident state 5.4 GB >> 129 MB L2", "parallelism": "replicas (one independent sim per GPU)"}
+    if extra:
+        d["sample"] = extra
+    return d
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return bench_reference(args)
+
+    rank, world, local, pg = dist_setup(args.gpus)
+    import torch
+
+    torch.cuda.set_device(local)
+    import __graft_entry__
+
+    if rank == 0 or not os.path.exists(os.path.join(ROOT, "luxum_gb300", "libluxum.so")):
+        __graft_entry__.build()
+    if pg:
+        pg.barrier()
+    from luxum_gb300 import Sim
+
+    p = workload_params(0)
+    sim = Sim(p)
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream.cuda_stream)
+    F = [material(sim.shape(c)) for c in range(3)]
+    for c in range(3):
+        sim.set_material(c, F[c], 1e6)
+    ijk = probe_points()
+    sim.set_probes(ijk, STEPS)
+    snap_bytes = [0]
+
+    def sink(t, comp, arr):
+        snap_bytes[0] += arr.nbytes
+
+    sim.set_snapshots(SNAP_EVERY, 0x3F, sink)
+
+    def one_run():
+        sim.reset()
+        sim.step(STEPS)
+
+    for _ in range(args.warmup):
+        one_run()
+    sim.sync()
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    k0 = sim.counters()[0]
+    with ClockSampler(local) as clk:
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            one_run()
+        sim.sync()
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    launches = sim.counters()[0] - k0
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    cell_updates = N ** 3 * STEPS * args.steps * world
+    value = cell_updates / (ms * 1e-3) / 1e9
+
+    # ---- end to end through the public API with pinned host buffers
+    Fp = []
+    for c in range(3):
+        buf = torch.empty(F[c].shape, dtype=torch.float64, pin_memory=True)
+        buf.numpy()[...] = F[c]
+        Fp.append(buf)
+    probe_host = np.empty((STEPS, 8, 6))
+    barrier()
+    _, h2d0, d2h0 = sim.counters()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    t_host = time.perf_counter()
+    e2.record(stream)
+    for _ in range(args.steps):
+        sim.reset()
+        for c in range(3):
+            sim.set_material(c, Fp[c].numpy(), 1e6)
+        sim.step(STEPS)
+        probe_host[...] = sim.probes()
+        sim.sync()
+    e3.record(stream)
+    barrier()
+    t_host = time.perf_counter() - t_host
+    ms_e2e = max(e2.elapsed_time(e3), 1e3 * t_host)
+    _, h2d1, d2h1 = sim.counters()
+    if pg:
+        t = torch.tensor([ms_e2e], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e = {"value": cell_updates / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": (h2d1 - h2d0) // args.steps, "d2h_bytes_per_step": (d2h1 - d2h0) // args.steps}
+
+    # ---- per-kernel roofline (instrumented pass, events around each launch)
+    sim.reset()
+    sim.step(120)  # wave inside the box, psi active
+    kt = sim.time_kernels(40)
+    model = kernel_model(sim, p)
+    dom = max(("h_update", "e_update"), key=lambda k: kt[k])
+    bytes_alg, flops_alg = model[dom]
+    peak_bw, peak_kind = measured_peaks()
+    achieved = bytes_alg / (kt[dom] * 1e-3) / 1e9
+    fp64_peak = fp64_peak_tflops(torch)
+    fp64_ach = flops_alg / (kt[dom] * 1e-3) / 1e12
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_bw, "unit": "GB/s", "frac": achieved / peak_bw,
+                "traffic": None, "kernel": dom, "peak_source": peak_kind,
+                "bytes_per_launch": bytes_alg, "ms_per_launch": kt[dom],
+                "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
+                         "flops_per_launch": flops_alg, "peak_source": "measured cuBLAS DGEMM 8192^3"},
+                "kernel_ms": kt}
+    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_file):
+        try:
+            with open(traffic_file) as f:
+                tr = json.load(f).get(dom)
+            if tr:
+                roofline["traffic"] = tr["bytes_per_launch"]
+                roofline["traffic_source"] = tr["source"]
+        except (OSError, ValueError):
+            pass
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_dict(),
+            "e2e": e2e, "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches,
+            "max_e2_final": sim.max_e2()}
+    sim.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, dt = run_cpu_sample(args.cpu_sample_steps, threads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{args.cpu_sample_steps} time steps of this workload "
+                                          f"({N ** 3 * args.cpu_sample_steps:.3g} cell-updates, {dt:.1f} s) run by "
+                                          "the oracle restatement of the reference's OpenMP loops"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

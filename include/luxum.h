@@ -177,13 +177,34 @@ typedef void (*lx_snapshot_fn)(void* user, int timestep, int comp, const double*
  * side stream and hands them to fn.  every = 0 disables. */
 LX_API lx_status lx_sim_set_snapshots(lx_sim* sim, int every, unsigned comp_mask, lx_snapshot_fn fn,
                                void* user);
-/* Same cadence, written to one HDF5 file per component in the layout of fileio.cc:60-212
- * (dataset "t=<step>", global staggered dims, native double, contiguous). */
-LX_API lx_status lx_sim_set_hdf5_output(lx_sim* sim, int every, int comp, const char* path);
+/* Adds an HDF5 file receiving component comp (LX_EX..LX_ETOTAL) at every step t with
+ * t >= first and t % every == 0, in the layout of fileio.cc:60-212 (dataset "t=<step>",
+ * global staggered dims, native double, contiguous).  The drivers' cadences: every 10
+ * (two_dim_pml.cc:184), every 20 from 100 (two_dim.cc:140), |E|^2 every 10
+ * (three_dim.cc:192) or every 3 (three_dim_pml.cc:279).  The file is complete after
+ * lx_sim_destroy. */
+LX_API lx_status lx_sim_set_hdf5_output(lx_sim* sim, int every, int first, int comp, const char* path);
+
+/* HDF5 files in the reference's layout (host only, no GPU).  lx_hdf5_write creates `path`
+ * with one 3-D native-double contiguous dataset per name (e.g. the material files that
+ * three_dim_pml.cc:109-118 reads, dataset "data").  lx_hdf5_read reads a little-endian
+ * float64/float32 dataset of rank <= 3 into `out` (n doubles, C order; out = NULL only
+ * queries the shape); shape is right-aligned, so rank 2 gives {1, n0, n1}.  Files with
+ * superblock 0/1, old-style groups and contiguous storage are supported (what fileio.cc
+ * writes and what h5py writes by default); chunked or compressed datasets are not. */
+LX_API lx_status lx_hdf5_write(const char* path, int ndatasets, const char* const* names, const double* const* data,
+                               const int shape[3]);
+LX_API lx_status lx_hdf5_read(const char* path, const char* dataset, double* out, size_t n, int shape[3]);
 
 /* Launch all device work of the handle on this CUDA stream (cudaStream_t) instead of its
  * own.  NULL restores the handle's own stream. */
 LX_API lx_status lx_sim_set_stream(lx_sim* sim, void* cuda_stream);
+
+/* Instrumented pass: runs nsteps steps with a CUDA event around every launch on the
+ * handle's stream and returns the mean device time per launch in milliseconds of
+ * out_ms[0] step prologue, [1] H-update kernel, [2] E-update kernel, [3] probe kernel
+ * (0 when that kernel did not run).  The steps advance the simulation like lx_sim_step. */
+LX_API lx_status lx_sim_time_kernels(lx_sim* sim, int nsteps, double out_ms[4]);
 
 /* Counters since creation: device kernels launched, bytes copied host->device and
  * device->host by the handle. */

@@ -88,9 +88,12 @@ def declare(lib) -> None:
     _proto(lib, "lx_sim_set_probes", C.c_int, sim, P(C.c_int), C.c_int, C.c_int)
     _proto(lib, "lx_sim_read_probes", C.c_int, sim, P(C.c_double), C.c_size_t, P(C.c_int))
     _proto(lib, "lx_sim_set_snapshots", C.c_int, sim, C.c_int, C.c_uint, SNAPSHOT_FN, C.c_void_p)
-    _proto(lib, "lx_sim_set_hdf5_output", C.c_int, sim, C.c_int, C.c_int, C.c_char_p)
+    _proto(lib, "lx_sim_set_hdf5_output", C.c_int, sim, C.c_int, C.c_int, C.c_int, C.c_char_p)
     _proto(lib, "lx_sim_set_stream", C.c_int, sim, C.c_void_p)
+    _proto(lib, "lx_sim_time_kernels", C.c_int, sim, C.c_int, P(C.c_double))
     _proto(lib, "lx_sim_counters", C.c_int, sim, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64))
+    _proto(lib, "lx_hdf5_write", C.c_int, C.c_char_p, C.c_int, P(C.c_char_p), P(P(C.c_double)), P(C.c_int))
+    _proto(lib, "lx_hdf5_read", C.c_int, C.c_char_p, C.c_char_p, P(C.c_double), C.c_size_t, P(C.c_int))
     _proto(lib, "lx_host_alloc", C.c_int, C.c_size_t, P(C.c_void_p))
     _proto(lib, "lx_host_free", None, C.c_void_p)
     _proto(lib, "lx_last_error", C.c_char_p, sim)

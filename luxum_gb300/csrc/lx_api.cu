@@ -739,7 +739,7 @@ static void writer_main(lx_sim* s) {
     if (e != cudaSuccess) err = std::string("snapshot copy: ") + cudaGetErrorString(e);
     if (err.empty()) {
       for (auto& o : s->outputs) {
-        if (o.every <= 0 || job.t % o.every != 0) continue;
+        if (o.every <= 0 || job.t < o.first || job.t % o.every != 0) continue;
         for (int c = 0; c < 7; c++) {
           if (!(o.mask & (1u << c)) || !(job.mask & (1u << c))) continue;
           const double* data = sl.host + job.off[c];
@@ -826,11 +826,13 @@ extern "C" LX_API lx_status lx_sim_set_snapshots(lx_sim* s, int every, unsigned 
   return add_output(s, o);
 }
 
-extern "C" LX_API lx_status lx_sim_set_hdf5_output(lx_sim* s, int every, int comp, const char* path) {
+extern "C" LX_API lx_status lx_sim_set_hdf5_output(lx_sim* s, int every, int first, int comp, const char* path) {
   if (!s || !path) return fail(s, LX_ERR_INVALID, "null argument");
-  if (every <= 0 || comp < 0 || comp > LX_ETOTAL || ext_n(s, comp) == 0) return fail(s, LX_ERR_INVALID, "bad cadence or component");
+  if (every <= 0 || first < 0 || comp < 0 || comp > LX_ETOTAL || ext_n(s, comp) == 0)
+    return fail(s, LX_ERR_INVALID, "bad cadence or component");
   lx::Output o;
   o.every = every;
+  o.first = first;
   o.mask = 1u << comp;
   o.h5 = new lx::Hdf5Writer();
   std::string m = o.h5->open(path, s->ext[comp]);
@@ -942,8 +944,15 @@ static lx::StepParams<T, C> step_params(lx_sim* s) {
   return p;
 }
 
+// Optional per-launch timing of run_steps (lx_sim_time_kernels).
+struct KernelTimer {
+  cudaEvent_t ev[2];
+  double sum[4] = {0, 0, 0, 0};
+  int cnt[4] = {0, 0, 0, 0};
+};
+
 template <class T, class C>
-static lx_status run_steps(lx_sim* s, int nsteps) {
+static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
   lx::StepParams<T, C> sp = step_params<T, C>(s);
   lx::PrologueParams pp;
   std::memset(&pp, 0, sizeof pp);
@@ -985,22 +994,45 @@ static lx_status run_steps(lx_sim* s, int nsteps) {
     bool mon = (q == nsteps - 1) || (s->p.monitor_every > 0 && (t + 1) % s->p.monitor_every == 0);
     unsigned snap = 0;
     for (auto& o : s->outputs)
-      if (o.every > 0 && t % o.every == 0) snap |= o.mask;
+      if (o.every > 0 && t >= o.first && t % o.every == 0) snap |= o.mask;
+    auto tic = [&]() -> lx_status {
+      if (kt) CK(cudaEventRecord(kt->ev[0], s->stream));
+      return LX_OK;
+    };
+    auto toc = [&](int which) -> lx_status {
+      if (!kt) return LX_OK;
+      CK(cudaEventRecord(kt->ev[1], s->stream));
+      CK(cudaEventSynchronize(kt->ev[1]));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, kt->ev[0], kt->ev[1]));
+      kt->sum[which] += ms;
+      kt->cnt[which]++;
+      return LX_OK;
+    };
+    lx_status st;
     if (pp.tab_total > 0 || s->src_kind >= 0 || mon) {
       pp.t = t;
       pp.max_slot = mon ? s->d_max : nullptr;
+      if ((st = tic())) return st;
       if (s->csize == 8) CK(lx::launch_prologue<double>(pp, s->stream));
       else CK(lx::launch_prologue<float>(pp, s->stream));
+      if ((st = toc(0))) return st;
       s->n_kernels++;
     }
+    if ((st = tic())) return st;
     CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, true, s->stream));
+    if ((st = toc(1))) return st;
     sp.max_slot = mon ? s->d_max : nullptr;
     sp.etotal = (snap & (1u << LX_ETOTAL)) ? (C*)s->etotal : nullptr;
+    if ((st = tic())) return st;
     CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, false, s->stream));
+    if ((st = toc(2))) return st;
     s->n_kernels += 2;
     if (s->nprobes > 0 && s->probe_rows < s->probe_cap) {
       prb.row = s->probe_rows++;
+      if ((st = tic())) return st;
       CK(lx::launch_probes<T>(prb, pf, s->d_probe, s->stream));
+      if ((st = toc(3))) return st;
       s->n_kernels++;
     }
     s->t++;
@@ -1040,6 +1072,22 @@ extern "C" LX_API lx_status lx_sim_step(lx_sim* s, int nsteps) {
   if (s->prec == LX_PREC_FP64) return run_steps<double, double>(s, nsteps);
   if (s->prec == LX_PREC_FP32) return run_steps<float, float>(s, nsteps);
   return run_steps<__half, float>(s, nsteps);
+}
+
+extern "C" LX_API lx_status lx_sim_time_kernels(lx_sim* s, int nsteps, double out_ms[4]) {
+  if (!s || !out_ms) return fail(s, LX_ERR_INVALID, "null argument");
+  if (nsteps < 1) return fail(s, LX_ERR_INVALID, "nsteps must be >= 1");
+  KernelTimer kt;
+  CK(cudaEventCreate(&kt.ev[0]));
+  CK(cudaEventCreate(&kt.ev[1]));
+  lx_status st;
+  if (s->prec == LX_PREC_FP64) st = run_steps<double, double>(s, nsteps, &kt);
+  else if (s->prec == LX_PREC_FP32) st = run_steps<float, float>(s, nsteps, &kt);
+  else st = run_steps<__half, float>(s, nsteps, &kt);
+  cudaEventDestroy(kt.ev[0]);
+  cudaEventDestroy(kt.ev[1]);
+  for (int q = 0; q < 4; q++) out_ms[q] = kt.cnt[q] ? kt.sum[q] / kt.cnt[q] : 0.0;
+  return st;
 }
 
 extern "C" LX_API int lx_sim_timestep(const lx_sim* s) { return s ? s->t : -1; }

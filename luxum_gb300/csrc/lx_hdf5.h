@@ -11,7 +11,8 @@ class Hdf5Writer {
  public:
   ~Hdf5Writer();
   std::string open(const char* path, const int ext[3]);
-  std::string write(int t, const double* data);
+  std::string write(int t, const double* data);  // dataset "t=<t>" (fileio.cc:186-187)
+  std::string write_named(const std::string& name, const double* data);
   std::string close();
 
  private:
@@ -24,5 +25,9 @@ class Hdf5Writer {
   unsigned long long eof_ = 0;
   std::vector<Entry> entries_;
 };
+
+// Reads a little-endian float64/float32 dataset of rank <= 3 (contiguous layout) of an HDF5
+// file with superblock 0/1; shape is right-aligned (rank 2 -> {1, n0, n1}).  Empty = ok.
+std::string hdf5_read(const char* path, const char* dataset, std::vector<double>& data, int shape[3]);
 
 }  // namespace lx

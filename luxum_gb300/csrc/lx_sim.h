@@ -19,6 +19,7 @@ class Hdf5Writer;  // lx_hdf5.cpp
 // One snapshot consumer: a user callback or an HDF5 file for one component.
 struct Output {
   int every = 0;
+  int first = 0;
   unsigned mask = 0;
   lx_snapshot_fn fn = nullptr;
   void* user = nullptr;

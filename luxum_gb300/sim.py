@@ -126,6 +126,12 @@ class Sim:
     def step(self, n: int = 1) -> None:
         self._check(self.lib.lx_sim_step(self.h, n))
 
+    def time_kernels(self, n: int) -> dict:
+        """Mean device ms per launch of each kernel over an instrumented pass of n steps."""
+        out = (C.c_double * 4)()
+        self._check(self.lib.lx_sim_time_kernels(self.h, n, out))
+        return {"prologue": out[0], "h_update": out[1], "e_update": out[2], "probes": out[3]}
+
     def sync(self) -> None:
         self._check(self.lib.lx_sim_sync(self.h))
 
@@ -166,5 +172,34 @@ class Sim:
         self._cb = _ffi.SNAPSHOT_FN(trampoline)
         self._check(self.lib.lx_sim_set_snapshots(self.h, every, mask, self._cb, None))
 
-    def set_hdf5_output(self, every: int, comp: int, path: str) -> None:
-        self._check(self.lib.lx_sim_set_hdf5_output(self.h, every, comp, str(path).encode()))
+    def set_hdf5_output(self, every: int, comp: int, path: str, first: int = 0) -> None:
+        self._check(self.lib.lx_sim_set_hdf5_output(self.h, every, first, comp, str(path).encode()))
+
+
+def hdf5_write(path: str, datasets: dict) -> None:
+    """Writes {name: 3-D float64 array} (all of one shape) as an HDF5 file in fileio.cc's layout."""
+    lib = _ffi.lib()
+    names = list(datasets)
+    arrs = [np.ascontiguousarray(datasets[n], dtype=np.float64) for n in names]
+    shape = arrs[0].shape if arrs else (0, 0, 0)
+    if any(a.shape != shape or a.ndim != 3 for a in arrs):
+        raise ValueError("all datasets must be 3-D arrays of one shape")
+    cnames = (C.c_char_p * len(names))(*[n.encode() for n in names])
+    ptrs = (C.POINTER(C.c_double) * len(arrs))(*[_dptr(a) for a in arrs])
+    st = lib.lx_hdf5_write(str(path).encode(), len(names), cnames, ptrs, (C.c_int * 3)(*shape))
+    if st:
+        raise LuxumError(st, lib.lx_last_error(None).decode())
+
+
+def hdf5_read(path: str, dataset: str) -> np.ndarray:
+    """Reads one float dataset (rank <= 3) of an HDF5 file; returns a 3-D array."""
+    lib = _ffi.lib()
+    shp = (C.c_int * 3)()
+    st = lib.lx_hdf5_read(str(path).encode(), dataset.encode(), None, 0, shp)
+    if st:
+        raise LuxumError(st, lib.lx_last_error(None).decode())
+    out = np.empty((shp[0], shp[1], shp[2]), dtype=np.float64)
+    st = lib.lx_hdf5_read(str(path).encode(), dataset.encode(), _dptr(out), out.size, shp)
+    if st:
+        raise LuxumError(st, lib.lx_last_error(None).decode())
+    return out
