@@ -42,14 +42,34 @@ BOX = (32, 223)
 CUBE = (104, 152)
 
 
-def workload_params(precision: int = 0):
+def workload_params(precision: int = 0, n: int = N):
+    """The 256^3 workload; n < 256 gives the same layout scaled down (profiling cases)."""
     from luxum_gb300 import params
 
-    return params(isPlanar=0, Nx=N, Ny=N, Nz=N, dx=1e-3, dy=1e-3, dz=1e-3, S=0.5, num_timesteps=STEPS,
+    box = (CPML + 16, n - 1 - (CPML + 16))
+    return params(isPlanar=0, Nx=n, Ny=n, Nz=n, dx=1e-3, dy=1e-3, dz=1e-3, S=0.5, num_timesteps=STEPS,
                   usePW=1, kx_pw=1.0, ky_pw=0.0, kz_pw=0.0, Ex_pw=0.0, Ey_pw=0.0, Ez_pw=1.0, off_pw=24.0,
-                  x1_pw=BOX[0], x2_pw=BOX[1], y1_pw=BOX[0], y2_pw=BOX[1], z1_pw=BOX[0], z2_pw=BOX[1],
+                  x1_pw=box[0], x2_pw=box[1], y1_pw=box[0], y2_pw=box[1], z1_pw=box[0], z2_pw=box[1],
                   usePML=1, d_pml=CPML * 1e-3, sigma=0.65, sigma_m=3.0, kappa=15.0, a_max=0.0, a_m=1.0,
                   precision=precision, n_threads=os.cpu_count() or 1)
+
+
+def profile_case(n: int, steps: int, precision: int) -> None:
+    """Small case for ncu captures: the workload at n^3 (n=192: 0.6 GB resident at FP64,
+    above the 129 MB L2), `steps` time steps after 60 untimed ones (wave inside the box)."""
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from luxum_gb300 import Sim
+
+    sim = Sim(workload_params(precision, n))
+    a, b = n * 104 // 256, n * 152 // 256
+    sim.set_eps_box((a, a, a), (b, b, b), 6.0)
+    sim.step(60)
+    sim.step(steps)
+    sim.sync()
+    print(json.dumps({"profile_case": n, "steps": 60 + steps, "precision": precision, "max_e2": sim.max_e2()}))
+    sim.close()
 
 
 def probe_points():
@@ -146,13 +166,11 @@ def kernel_model(sim, p):
     read and written once.  Flops per component: 3 differences + 1 FMA (5 flops); per psi
     term: psi = b*psi + c*d and d/kappa + psi (5 flops).
     """
-    el = 8 if p.precision == 0 else (4 if p.precision == 1 else 2)
+    info = sim.info()
+    el = info["field_bytes"]
     cel = 8 if p.precision == 0 else 4
-    cells = N ** 3
-    slab = 2 * CPML  # slab depth per axis with the 16-cell CPML
-    psi_axis = slab * N * N
-    psi_h = 2 * 3 * psi_axis  # two H components per axis x three axes
-    psi_e = 2 * 3 * psi_axis
+    cells = info["cells"]
+    psi_h, psi_e = info["psi_h_entries"], info["psi_e_entries"]
     h_bytes = cells * 9 * el + psi_h * 2 * cel
     e_bytes = cells * 9 * el + cells * 3 * cel + psi_e * 2 * cel
     h_flops = cells * 15 + psi_h * 5
@@ -237,7 +255,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", type=int, default=0, metavar="N",
+                    help="run the N^3 profiling case instead of the benchmark (for ncu)")
+    ap.add_argument("--profile-steps", type=int, default=4)
+    ap.add_argument("--precision", type=int, default=0, help="profiling case precision: 0 fp64, 1 fp32, 2 fp16")
     args = ap.parse_args()
+    if args.profile:
+        return profile_case(args.profile, args.profile_steps, args.precision)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -167,6 +167,21 @@ LX_API lx_status lx_sim_set_probes(lx_sim* sim, const int* ijk, int nprobes, int
 /* Copies [nsteps recorded][nprobes][6] doubles; *nsteps_out receives the row count. */
 LX_API lx_status lx_sim_read_probes(lx_sim* sim, double* host, size_t n, int* nsteps_out);
 
+/* Frequency-domain plane monitor (engine feature; the reference has none).  Keeps FP64
+ * running DFTs, at nfreq angular frequencies omega[f] (rad/s), of the four field components
+ * tangential to the plane normal to `axis` (0 x, 1 y, 2 z) through cell index `index`:
+ * (E_t1, E_t2, H_t1, H_t2) with (t1, t2) = (y, z), (z, x) or (x, y).  After the E update of
+ * every step t with t % every == 0 it adds every * E(t+1) e^{-i omega (t+1) dt} and
+ * every * H(t+1/2) e^{-i omega (t+1/2) dt}; all four are sampled at the plane's cell (i,j,k)
+ * (0 outside a component's extent).  Planar grids: the plane is a line, axis 0 or 2. */
+LX_API lx_status lx_sim_add_dft_plane(lx_sim* sim, int axis, int index, int nfreq, const double* omega, int every,
+                                      int* id);
+/* Raw accumulators [nfreq][4][na][nb][2] (re, im), (na, nb) = in-plane extents in axis order. */
+LX_API lx_status lx_sim_read_dft(lx_sim* sim, int id, double* host, size_t n);
+/* Net power flux through the plane per frequency: sum over cells of
+ * Re(E_t1 conj(H_t2) - E_t2 conj(H_t1)) times the cell face area (planar: the cell edge). */
+LX_API lx_status lx_sim_dft_flux(lx_sim* sim, int id, double* flux, int nfreq);
+
 /* Snapshot callback: called from the handle's writer thread, in step order, with a host
  * buffer valid only during the call. */
 typedef void (*lx_snapshot_fn)(void* user, int timestep, int comp, const double* data,
@@ -205,6 +220,18 @@ LX_API lx_status lx_sim_set_stream(lx_sim* sim, void* cuda_stream);
  * out_ms[0] step prologue, [1] H-update kernel, [2] E-update kernel, [3] probe kernel
  * (0 when that kernel did not run).  The steps advance the simulation like lx_sim_step. */
 LX_API lx_status lx_sim_time_kernels(lx_sim* sim, int nsteps, double out_ms[4]);
+
+/* Sizes of a handle's device state (engine feature). */
+typedef struct lx_info {
+  size_t cells;          /* Nx*Ny*Nz */
+  size_t device_bytes;   /* device memory held by the handle now */
+  size_t psi_h_entries;  /* stored CPML psi entries updated by the H kernel */
+  size_t psi_e_entries;  /* ... by the E kernel */
+  int slab[3];           /* stored psi depth per axis (0: no CPML on that axis) */
+  int uniform;           /* 1 when dx = dy = dz (curls kept as plain differences) */
+  int field_bytes;       /* bytes per stored field value (8, 4 or 2) */
+} lx_info;
+LX_API lx_status lx_sim_info(const lx_sim* sim, lx_info* info);
 
 /* Counters since creation: device kernels launched, bytes copied host->device and
  * device->host by the handle. */

@@ -55,6 +55,11 @@ class Params(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class Info(C.Structure):
+    _fields_ = [("cells", C.c_size_t), ("device_bytes", C.c_size_t), ("psi_h_entries", C.c_size_t),
+                ("psi_e_entries", C.c_size_t), ("slab", C.c_int * 3), ("uniform", C.c_int), ("field_bytes", C.c_int)]
+
+
 SNAPSHOT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int))
 
 _lib = None
@@ -87,10 +92,14 @@ def declare(lib) -> None:
     _proto(lib, "lx_sim_max_e2", C.c_int, sim, P(C.c_double))
     _proto(lib, "lx_sim_set_probes", C.c_int, sim, P(C.c_int), C.c_int, C.c_int)
     _proto(lib, "lx_sim_read_probes", C.c_int, sim, P(C.c_double), C.c_size_t, P(C.c_int))
+    _proto(lib, "lx_sim_add_dft_plane", C.c_int, sim, C.c_int, C.c_int, C.c_int, P(C.c_double), C.c_int, P(C.c_int))
+    _proto(lib, "lx_sim_read_dft", C.c_int, sim, C.c_int, P(C.c_double), C.c_size_t)
+    _proto(lib, "lx_sim_dft_flux", C.c_int, sim, C.c_int, P(C.c_double), C.c_int)
     _proto(lib, "lx_sim_set_snapshots", C.c_int, sim, C.c_int, C.c_uint, SNAPSHOT_FN, C.c_void_p)
     _proto(lib, "lx_sim_set_hdf5_output", C.c_int, sim, C.c_int, C.c_int, C.c_int, C.c_char_p)
     _proto(lib, "lx_sim_set_stream", C.c_int, sim, C.c_void_p)
     _proto(lib, "lx_sim_time_kernels", C.c_int, sim, C.c_int, P(C.c_double))
+    _proto(lib, "lx_sim_info", C.c_int, sim, P(Info))
     _proto(lib, "lx_sim_counters", C.c_int, sim, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64))
     _proto(lib, "lx_hdf5_write", C.c_int, C.c_char_p, C.c_int, P(C.c_char_p), P(P(C.c_double)), P(C.c_int))
     _proto(lib, "lx_hdf5_read", C.c_int, C.c_char_p, C.c_char_p, P(C.c_double), C.c_size_t, P(C.c_int))

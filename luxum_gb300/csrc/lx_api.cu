@@ -348,6 +348,10 @@ extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
     if (sl.ev_d2h) cudaEventDestroy(sl.ev_d2h);
   }
   for (auto& o : s->outputs) delete o.h5;
+  for (auto& d : s->dfts) {
+    cudaFree(d.d_omega);
+    cudaFree(d.d_acc);
+  }
   if (s->own) cudaStreamDestroy(s->own);
   if (s->side) cudaStreamDestroy(s->side);
   delete s;
@@ -548,6 +552,7 @@ extern "C" LX_API lx_status lx_sim_reset(lx_sim* s) {
     }
   }
   if (s->etotal) CK(cudaMemsetAsync(s->etotal, 0, s->ncell * s->csize, s->stream));
+  for (auto& d : s->dfts) CK(cudaMemsetAsync(d.d_acc, 0, d.n_acc * sizeof(double), s->stream));
   s->t = 0;
   s->probe_rows = 0;
   s->last_max = 0.0;
@@ -717,6 +722,73 @@ extern "C" LX_API lx_status lx_sim_read_probes(lx_sim* s, double* host, size_t n
   CK(cudaMemcpyAsync(host, s->d_probe, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   s->n_d2h += m * sizeof(double);
+  return LX_OK;
+}
+
+// ------------------------------------------------------------------ DFT plane monitors
+
+extern "C" LX_API lx_status lx_sim_add_dft_plane(lx_sim* s, int axis, int index, int nfreq, const double* omega,
+                                                 int every, int* id) {
+  if (!s || !omega || !id) return fail(s, LX_ERR_INVALID, "null argument");
+  if (axis < 0 || axis > 2 || (s->planar && axis == 1)) return fail(s, LX_ERR_INVALID, "axis must be 0, 1 or 2 (planar: 0 or 2)");
+  const int N[3] = {s->Nx, s->Ny, s->Nz};
+  if (index < 0 || index >= N[axis]) return fail(s, LX_ERR_INVALID, "plane index outside the grid");
+  if (nfreq < 1 || nfreq > lx::kMaxDftFreq || every < 1) return fail(s, LX_ERR_INVALID, "1..256 frequencies, every >= 1");
+  static const int kComps[3][4] = {{LX_EY, LX_EZ, LX_HY, LX_HZ}, {LX_EZ, LX_EX, LX_HZ, LX_HX}, {LX_EX, LX_EY, LX_HX, LX_HY}};
+  lx::DftPlane d;
+  d.axis = axis;
+  d.index = index;
+  d.nfreq = nfreq;
+  d.every = every;
+  d.na = axis == 0 ? s->Ny : s->Nx;
+  d.nb = axis == 2 ? s->Ny : s->Nz;
+  for (int q = 0; q < 4; q++) d.comps[q] = kComps[axis][q];
+  d.omega.assign(omega, omega + nfreq);
+  d.n_acc = (size_t)nfreq * 4 * d.na * d.nb * 2;
+  CK(cudaMalloc(&d.d_omega, nfreq * sizeof(double)));
+  CK(cudaMemcpy(d.d_omega, omega, nfreq * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&d.d_acc, d.n_acc * sizeof(double)));
+  CK(cudaMemset(d.d_acc, 0, d.n_acc * sizeof(double)));
+  s->n_h2d += nfreq * sizeof(double);
+  s->dfts.push_back(d);
+  *id = (int)s->dfts.size() - 1;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_read_dft(lx_sim* s, int id, double* host, size_t n) {
+  if (!s || !host) return fail(s, LX_ERR_INVALID, "null argument");
+  if (id < 0 || id >= (int)s->dfts.size()) return fail(s, LX_ERR_INVALID, "no such DFT plane");
+  const lx::DftPlane& d = s->dfts[id];
+  if (n != d.n_acc) return fail(s, LX_ERR_INVALID, "buffer size must be nfreq*4*na*nb*2");
+  CK(cudaMemcpyAsync(host, d.d_acc, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_d2h += n * sizeof(double);
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_dft_flux(lx_sim* s, int id, double* flux, int nfreq) {
+  if (!s || !flux) return fail(s, LX_ERR_INVALID, "null argument");
+  if (id < 0 || id >= (int)s->dfts.size()) return fail(s, LX_ERR_INVALID, "no such DFT plane");
+  const lx::DftPlane& d = s->dfts[id];
+  if (nfreq != d.nfreq) return fail(s, LX_ERR_INVALID, "nfreq does not match the plane");
+  std::vector<double> acc(d.n_acc);
+  lx_status st = lx_sim_read_dft(s, id, acc.data(), acc.size());
+  if (st) return st;
+  const double sp[3] = {s->p.dx, s->p.dy, s->p.dz};
+  double dA;
+  if (s->planar) dA = d.axis == 0 ? sp[2] : sp[0];
+  else dA = d.axis == 0 ? sp[1] * sp[2] : (d.axis == 1 ? sp[2] * sp[0] : sp[0] * sp[1]);
+  const size_t nc = (size_t)d.na * d.nb;
+  for (int f = 0; f < d.nfreq; f++) {
+    const double* e1 = &acc[((size_t)f * 4 + 0) * nc * 2];
+    const double* e2 = &acc[((size_t)f * 4 + 1) * nc * 2];
+    const double* h1 = &acc[((size_t)f * 4 + 2) * nc * 2];
+    const double* h2 = &acc[((size_t)f * 4 + 3) * nc * 2];
+    double sum = 0.0;
+    for (size_t q = 0; q < nc; q++)
+      sum += (e1[2 * q] * h2[2 * q] + e1[2 * q + 1] * h2[2 * q + 1]) - (e2[2 * q] * h1[2 * q] + e2[2 * q + 1] * h1[2 * q + 1]);
+    flux[f] = sum * dA;
+  }
   return LX_OK;
 }
 
@@ -1028,6 +1100,21 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
     CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, false, s->stream));
     if ((st = toc(2))) return st;
     s->n_kernels += 2;
+    for (auto& d : s->dfts) {
+      if (t % d.every != 0) continue;
+      lx::DftParams dp;
+      std::memset(&dp, 0, sizeof dp);
+      dp.axis = d.axis; dp.index = d.index; dp.na = d.na; dp.nb = d.nb; dp.Ny = s->Ny; dp.Nzp = s->Nzp;
+      dp.nfreq = d.nfreq; dp.t = t; dp.dt = s->k.dt; dp.weight = (double)d.every;
+      dp.omega = d.d_omega; dp.acc = d.d_acc;
+      T* f4[4];
+      for (int q = 0; q < 4; q++) {
+        f4[q] = pf[d.comps[q]];
+        for (int a = 0; a < 3; a++) dp.ext[q][a] = s->ext[d.comps[q]][a];
+      }
+      CK(lx::launch_dft<T>(dp, f4, s->stream));
+      s->n_kernels++;
+    }
     if (s->nprobes > 0 && s->probe_rows < s->probe_cap) {
       prb.row = s->probe_rows++;
       if ((st = tic())) return st;
@@ -1103,6 +1190,33 @@ extern "C" LX_API lx_status lx_sim_set_stream(lx_sim* s, void* stream) {
   lx_status st = lx_sim_sync(s);
   if (st) return st;
   s->stream = stream ? (cudaStream_t)stream : s->own;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_info(const lx_sim* s, lx_info* info) {
+  if (!s || !info) return fail((lx_sim*)s, LX_ERR_INVALID, "null argument");
+  std::memset(info, 0, sizeof *info);
+  info->cells = (size_t)s->Nx * s->Ny * s->Nz;
+  size_t b = 0;
+  for (int c = 0; c < 3; c++) {
+    if (s->E[c]) b += s->ncell * s->tsize;
+    if (s->H[c]) b += s->ncell * s->tsize;
+    if (s->Cbs[c]) b += s->ncell * s->csize;
+    for (int q = 0; q < 2; q++) {
+      info->psi_h_entries += s->psiH_n[c][q];
+      info->psi_e_entries += s->psiE_n[c][q];
+    }
+  }
+  b += (info->psi_h_entries + info->psi_e_entries) * s->csize;
+  if (s->etotal) b += s->ncell * s->csize;
+  b += s->xfer_cap * sizeof(double) + (size_t)s->tab_total * s->csize;
+  for (auto& sl : s->slots) b += sl.cap * sizeof(double);
+  for (auto& d : s->dfts) b += d.n_acc * sizeof(double);
+  b += (size_t)s->probe_cap * s->nprobes * 6 * sizeof(double);
+  info->device_bytes = b;
+  for (int a = 0; a < 3; a++) info->slab[a] = s->pml ? s->slab[a].n : 0;
+  info->uniform = s->uniform;
+  info->field_bytes = (int)s->tsize;
   return LX_OK;
 }
 

@@ -23,6 +23,7 @@
 namespace lx {
 
 constexpr int kMaxProbes = 64;
+constexpr int kMaxDftFreq = 256;
 
 // Packed CPML slab along one axis.
 struct Slab {
@@ -113,6 +114,15 @@ struct ProbeParams {
   int nprobes, row, Ny, Nzp;
   int ext[6][3];    // staggered extents of the six components (0 for absent ones)
   const int* ijk;   // device array [nprobes][3]
+};
+
+// One DFT plane monitor (see lx_sim_add_dft_plane).
+struct DftParams {
+  int axis, index, na, nb, Ny, Nzp, nfreq, t;
+  int ext[4][3];          // extents of the four sampled components
+  double dt, weight;
+  const double* omega;    // device [nfreq]
+  double* acc;            // device [nfreq][4][na*nb][2]
 };
 
 }  // namespace lx

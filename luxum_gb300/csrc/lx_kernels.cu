@@ -484,6 +484,47 @@ __global__ void probe_kernel(const ProbeParams pp, const T* f0, const T* f1, con
   out[(long long)pp.row * pp.nprobes * 6 + q] = v;
 }
 
+// Running DFT of the four tangential components on one plane.  Each block evaluates the
+// phase factors of every frequency once into shared memory; each thread owns one
+// (component, cell) and updates its nfreq complex accumulators (coalesced along the cell).
+template <class T>
+__global__ void dft_kernel(const DftParams d, const T* f0, const T* f1, const T* f2, const T* f3) {
+  __shared__ double cs[2][kMaxDftFreq], sn[2][kMaxDftFreq];
+  for (int f = threadIdx.x; f < d.nfreq; f += blockDim.x) {
+    const double pe = __dmul_rn(d.omega[f], __dmul_rn((double)(d.t + 1), d.dt));
+    const double ph = __dmul_rn(d.omega[f], __dmul_rn((double)d.t + 0.5, d.dt));
+    sincos(pe, &sn[0][f], &cs[0][f]);
+    sincos(ph, &sn[1][f], &cs[1][f]);
+  }
+  __syncthreads();
+  const long long ncell = (long long)d.na * d.nb;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= 4 * ncell) return;
+  const int comp = (int)(q / ncell);
+  const long long cell = q % ncell;
+  const int a = (int)(cell / d.nb), b = (int)(cell % d.nb);
+  int u[3];
+  u[d.axis] = d.index;
+  u[d.axis == 0 ? 1 : 0] = a;
+  u[d.axis == 2 ? 1 : 2] = b;
+  const T* f = comp == 0 ? f0 : comp == 1 ? f1 : comp == 2 ? f2 : f3;
+  double v = 0.0;
+  if (f && u[0] < d.ext[comp][0] && u[1] < d.ext[comp][1] && u[2] < d.ext[comp][2]) {
+    const T* src = f + ((long long)u[0] * d.Ny + u[1]) * d.Nzp + u[2];
+    if constexpr (sizeof(T) == 2) v = (double)__half2float(*src);
+    else v = (double)*src;
+  }
+  v = __dmul_rn(v, d.weight);
+  const int w = comp < 2 ? 0 : 1;
+  double2* acc = reinterpret_cast<double2*>(d.acc);
+  for (int fq = 0; fq < d.nfreq; ++fq) {
+    double2 x = acc[((long long)fq * 4 + comp) * ncell + cell];
+    x.x = fma(v, cs[w][fq], x.x);
+    x.y = fma(-v, sn[w][fq], x.y);
+    acc[((long long)fq * 4 + comp) * ncell + cell] = x;
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 
 static inline unsigned grid1d(long long n, int bs) {
@@ -556,12 +597,20 @@ cudaError_t launch_probes(const ProbeParams& pp, T* const f[6], double* out, cud
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s) {
+  const long long n = 4LL * d.na * d.nb;
+  dft_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, f[0], f[1], f[2], f[3]);
+  return cudaGetLastError();
+}
+
 #define LX_INST(T, C)                                                                                                  \
   template cudaError_t launch_step<T, C>(const StepParams<T, C>&, bool, bool, bool, cudaStream_t);                   \
   template cudaError_t launch_gather<T>(const T*, double*, const int[3], int, int, cudaStream_t);                     \
   template cudaError_t launch_scatter<T>(const double*, T*, const int[3], int, int, int, double, double, double,      \
                                          double, cudaStream_t);                                                        \
-  template cudaError_t launch_probes<T>(const ProbeParams&, T* const[6], double*, cudaStream_t);
+  template cudaError_t launch_probes<T>(const ProbeParams&, T* const[6], double*, cudaStream_t);                   \
+  template cudaError_t launch_dft<T>(const DftParams&, T* const[4], cudaStream_t);
 LX_INST(double, double)
 LX_INST(float, float)
 LX_INST(__half, float)

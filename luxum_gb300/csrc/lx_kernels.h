@@ -21,4 +21,7 @@ cudaError_t launch_eps_box(C* dst, const int ext[3], int Ny, int Nzp, const int 
 template <class T>
 cudaError_t launch_probes(const ProbeParams& pp, T* const f[6], double* out, cudaStream_t s);
 
+template <class T>
+cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s);
+
 }  // namespace lx

@@ -35,6 +35,15 @@ struct SnapSlot {
   bool busy = false;
 };
 
+struct DftPlane {
+  int axis = 0, index = 0, nfreq = 0, every = 1, na = 0, nb = 0;
+  int comps[4] = {0, 0, 0, 0};
+  std::vector<double> omega;
+  double* d_omega = nullptr;
+  double* d_acc = nullptr;
+  size_t n_acc = 0;  // doubles
+};
+
 struct SnapJob {
   int slot, t;
   unsigned mask;
@@ -91,6 +100,8 @@ struct lx_sim {
   int nprobes = 0, probe_cap = 0, probe_rows = 0;
   int* d_probe_ijk = nullptr;
   double* d_probe = nullptr;
+  // DFT plane monitors
+  std::vector<lx::DftPlane> dfts;
   // snapshots
   std::vector<lx::Output> outputs;
   lx::SnapSlot slots[2];

@@ -93,6 +93,13 @@ class Sim:
         self._check(self.lib.lx_sim_max_e2(self.h, C.byref(v)))
         return v.value
 
+    def info(self) -> dict:
+        i = _ffi.Info()
+        self._check(self.lib.lx_sim_info(self.h, C.byref(i)))
+        return {"cells": i.cells, "device_bytes": i.device_bytes, "psi_h_entries": i.psi_h_entries,
+                "psi_e_entries": i.psi_e_entries, "slab": list(i.slab), "uniform": i.uniform,
+                "field_bytes": i.field_bytes}
+
     def counters(self) -> tuple[int, int, int]:
         k, a, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
         self._check(self.lib.lx_sim_counters(self.h, C.byref(k), C.byref(a), C.byref(b)))
@@ -155,6 +162,31 @@ class Sim:
         rows = C.c_int()
         self._check(self.lib.lx_sim_read_probes(self.h, _dptr(out), out.size, C.byref(rows)))
         return out[: rows.value, :n]
+
+    def add_dft_plane(self, axis: int, index: int, omega, every: int = 1) -> int:
+        w = np.ascontiguousarray(omega, dtype=np.float64)
+        i = C.c_int()
+        self._check(self.lib.lx_sim_add_dft_plane(self.h, axis, index, w.size, _dptr(w), every, C.byref(i)))
+        n = [self.shape(0), self.shape(1), self.shape(2)]
+        N = (self.p.Nx, 1 if self.p.isPlanar else self.p.Ny, self.p.Nz)
+        na = N[1] if axis == 0 else N[0]
+        nb = N[1] if axis == 2 else N[2]
+        self._dft = getattr(self, "_dft", {})
+        self._dft[i.value] = (w.size, na, nb)
+        return i.value
+
+    def dft(self, plane: int) -> np.ndarray:
+        """Complex accumulators [nfreq, 4, na, nb] of one DFT plane."""
+        nf, na, nb = self._dft[plane]
+        raw = np.empty((nf, 4, na, nb, 2))
+        self._check(self.lib.lx_sim_read_dft(self.h, plane, _dptr(raw), raw.size))
+        return raw[..., 0] + 1j * raw[..., 1]
+
+    def dft_flux(self, plane: int) -> np.ndarray:
+        nf = self._dft[plane][0]
+        out = np.empty(nf)
+        self._check(self.lib.lx_sim_dft_flux(self.h, plane, _dptr(out), nf))
+        return out
 
     def set_snapshots(self, every: int, mask: int, fn: Callable[[int, int, np.ndarray], None] | None) -> None:
         """fn(t, comp, array) is called from the handle's writer thread with a copy."""

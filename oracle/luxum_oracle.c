@@ -48,6 +48,16 @@ typedef struct {
   int face; /* isFaceCentered */
 } vf;
 
+/* extension: running-DFT plane monitor (see lx_sim_add_dft_plane in include/luxum.h) */
+typedef struct {
+  int axis, index, nfreq, every, na, nb;
+  int comp[4];
+  double* omega;
+  double* acc; /* [nfreq][4][na*nb][2] */
+} ox_dft;
+
+#define OX_MAX_DFT 16
+
 typedef struct ox_sim {
   lx_params p;
   int planar, pml, threads;
@@ -69,6 +79,9 @@ typedef struct ox_sim {
   int nprobes, probe_cap, probe_rows;
   int* probe_ijk;
   double* probe_buf;
+  /* DFT planes (extension) */
+  int ndft;
+  ox_dft dft[OX_MAX_DFT];
 } ox_sim;
 
 void ox_destroy(struct ox_sim* s);
@@ -422,6 +435,10 @@ void ox_destroy(ox_sim* s) {
   }
   free(s->probe_ijk);
   free(s->probe_buf);
+  for (int q = 0; q < s->ndft; q++) {
+    free(s->dft[q].omega);
+    free(s->dft[q].acc);
+  }
   free(s);
 }
 
@@ -1034,6 +1051,64 @@ static void record_probes(ox_sim* s) {
   s->probe_rows++;
 }
 
+int ox_add_dft_plane(ox_sim* s, int axis, int index, int nfreq, const double* omega, int every) {
+  static const int comps[3][4] = {{LX_EY, LX_EZ, LX_HY, LX_HZ}, {LX_EZ, LX_EX, LX_HZ, LX_HX}, {LX_EX, LX_EY, LX_HX, LX_HY}};
+  if (s->ndft >= OX_MAX_DFT || axis < 0 || axis > 2 || (s->planar && axis == 1) || nfreq < 1 || every < 1) return -1;
+  int N[3] = {s->Nx, s->Ny, s->Nz};
+  if (index < 0 || index >= N[axis]) return -1;
+  ox_dft* d = &s->dft[s->ndft];
+  d->axis = axis; d->index = index; d->nfreq = nfreq; d->every = every;
+  d->na = axis == 0 ? s->Ny : s->Nx;
+  d->nb = axis == 2 ? s->Ny : s->Nz;
+  for (int q = 0; q < 4; q++) d->comp[q] = comps[axis][q];
+  d->omega = (double*)malloc(sizeof(double) * (size_t)nfreq);
+  d->acc = (double*)calloc((size_t)nfreq * 4 * d->na * d->nb * 2, sizeof(double));
+  if (!d->omega || !d->acc) return -1;
+  memcpy(d->omega, omega, sizeof(double) * (size_t)nfreq);
+  return s->ndft++;
+}
+
+int ox_read_dft(ox_sim* s, int id, double* out, size_t n) {
+  if (id < 0 || id >= s->ndft) return LX_ERR_INVALID;
+  ox_dft* d = &s->dft[id];
+  size_t m = (size_t)d->nfreq * 4 * d->na * d->nb * 2;
+  if (n != m) return LX_ERR_INVALID;
+  memcpy(out, d->acc, m * sizeof(double));
+  return LX_OK;
+}
+
+/* acc += every * F(t+1) e^{-i w (t+1) dt} for E, every * F(t+1/2) e^{-i w (t+1/2) dt} for H */
+static void record_dft(ox_sim* s, int t) {
+  for (int q = 0; q < s->ndft; q++) {
+    ox_dft* d = &s->dft[q];
+    if (t % d->every != 0) continue;
+    size_t nc = (size_t)d->na * d->nb;
+    for (int comp = 0; comp < 4; comp++) {
+      arr3* f = comp_arr(s, d->comp[comp]);
+      int sh[3];
+      ox_field_shape(s, d->comp[comp], sh);
+      for (int fq = 0; fq < d->nfreq; fq++) {
+        double ph = comp < 2 ? d->omega[fq] * ((double)(t + 1) * s->dt) : d->omega[fq] * (((double)t + 0.5) * s->dt);
+        double c = cos(ph), sn = sin(ph);
+        double* acc = d->acc + ((size_t)fq * 4 + comp) * nc * 2;
+        for (int a = 0; a < d->na; a++)
+          for (int b = 0; b < d->nb; b++) {
+            int u[3];
+            u[d->axis] = d->index;
+            u[d->axis == 0 ? 1 : 0] = a;
+            u[d->axis == 2 ? 1 : 2] = b;
+            double v = 0.0;
+            if (u[0] < sh[0] && u[1] < sh[1] && u[2] < sh[2]) v = A3(*f, u[0], u[1], u[2]);
+            v = v * (double)d->every;
+            size_t cell = (size_t)a * d->nb + b;
+            acc[2 * cell] = fma(v, c, acc[2 * cell]);
+            acc[2 * cell + 1] = fma(-v, sn, acc[2 * cell + 1]);
+          }
+      }
+    }
+  }
+}
+
 /* maxwell::solve_planar two_dim.cc:85-144 (one iteration) */
 static void step_planar(ox_sim* s, int t) {
   int Nx = s->Nx, Nz = s->Nz, nt = s->threads;
@@ -1218,6 +1293,7 @@ int ox_step(ox_sim* s, int nsteps) {
       else step_3d(s, t);
     }
     s->t++;
+    record_dft(s, t);
     record_probes(s);
   }
   return LX_OK;

@@ -39,6 +39,8 @@ def lib():
             ("ox_set_probes", C.c_int, [C.c_void_p, P(C.c_int), C.c_int, C.c_int]),
             ("ox_read_probes", C.c_int, [C.c_void_p, P(C.c_double), C.c_size_t, P(C.c_int)]),
             ("ox_step", C.c_int, [C.c_void_p, C.c_int]),
+            ("ox_add_dft_plane", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, P(C.c_double), C.c_int]),
+            ("ox_read_dft", C.c_int, [C.c_void_p, C.c_int, P(C.c_double), C.c_size_t]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -67,6 +69,7 @@ class OracleSim:
         if st:
             raise OracleError(st)
         self.h = h
+        self._p = p
         self.L.ox_set_threads(h, threads)
         self._np = 0
         self._cap = 0
@@ -127,6 +130,21 @@ class OracleSim:
         assert self.L.ox_set_probes(self.h, a.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], capacity) == 0
         self._np = a.shape[0]
         self._cap = capacity
+
+    def add_dft_plane(self, axis, index, omega, every=1):
+        w = np.ascontiguousarray(omega, dtype=np.float64)
+        i = self.L.ox_add_dft_plane(self.h, axis, index, w.size, _dptr(w), every)
+        assert i >= 0
+        N = (self._p.Nx, 1 if self._p.isPlanar else self._p.Ny, self._p.Nz)
+        self._dft = getattr(self, "_dft", {})
+        self._dft[i] = (w.size, N[1] if axis == 0 else N[0], N[1] if axis == 2 else N[2])
+        return i
+
+    def dft(self, plane):
+        nf, na, nb = self._dft[plane]
+        raw = np.empty((nf, 4, na, nb, 2))
+        assert self.L.ox_read_dft(self.h, plane, _dptr(raw), raw.size) == 0
+        return raw[..., 0] + 1j * raw[..., 1]
 
     def probes(self):
         out = np.zeros((max(self._cap, 1), max(self._np, 1), 6))

@@ -81,3 +81,22 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     if nb == 0.0:
         return 0.0 if na == 0.0 else float("inf")
     return na / nb
+
+
+def field_errors(get_a, get_b, shapes):
+    """Per-component error relative to the norm of its field group (E or H).
+
+    A component can be pure cancellation noise (e.g. Hz of a z-directed point source is
+    ~1e-16 of |H|); measuring it against its own norm would be meaningless, so every
+    component's error is taken relative to ||E|| or ||H|| of the reference solution.
+    Returns {component: error}.
+    """
+    out = {}
+    for group in ((0, 1, 2), (3, 4, 5)):
+        comps = [c for c in group if np.prod(shapes[c]) > 0]
+        bs = {c: get_b(c) for c in comps}
+        gn = float(np.sqrt(sum(np.linalg.norm(b) ** 2 for b in bs.values())))
+        for c in comps:
+            d = float(np.linalg.norm(get_a(c) - bs[c]))
+            out[c] = d / gn if gn > 0 else (0.0 if d == 0 else float("inf"))
+    return out
