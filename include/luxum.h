@@ -211,6 +211,26 @@ LX_API lx_status lx_hdf5_write(const char* path, int ndatasets, const char* cons
                                const int shape[3]);
 LX_API lx_status lx_hdf5_read(const char* path, const char* dataset, double* out, size_t n, int shape[3]);
 
+/* ---- batches: many independent simulations stepped together (engine feature) ----
+ * Member handles keep their own device state; each step runs one prologue launch, one H and
+ * one E launch per group of members sharing (planar, uniform spacing) over a tile table of
+ * all of them, one launch for every member's DFT planes and a step-counter tick.  Chunks of
+ * steps are captured once as a CUDA graph and replayed.  All members share one precision;
+ * members may not have snapshot outputs or probes (use lx_sim_step for those).  max|E|^2
+ * is monitored every step.  A handle belongs to at most one batch; lx_sim_step on a member
+ * is allowed between batch steps (the batch re-reads its step counter). */
+typedef struct lx_batch lx_batch;
+LX_API lx_status lx_batch_create(lx_batch** out);
+LX_API void lx_batch_destroy(lx_batch* b); /* does not destroy the members */
+LX_API lx_status lx_batch_add(lx_batch* b, lx_sim* sim);
+LX_API lx_status lx_batch_remove(lx_batch* b, lx_sim* sim);
+LX_API int lx_batch_size(const lx_batch* b);
+/* Steps between CUDA-graph captures (default 100; 0 launches without graphs). */
+LX_API lx_status lx_batch_set_chunk(lx_batch* b, int steps);
+/* Advances every member by nsteps; returns LX_ERR_BLOWUP if any member's max|E|^2 is not
+ * finite afterwards (lx_last_error(NULL) names the first such member). */
+LX_API lx_status lx_batch_step(lx_batch* b, int nsteps);
+
 /* Launch all device work of the handle on this CUDA stream (cudaStream_t) instead of its
  * own.  NULL restores the handle's own stream. */
 LX_API lx_status lx_sim_set_stream(lx_sim* sim, void* cuda_stream);

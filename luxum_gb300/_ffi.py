@@ -103,6 +103,13 @@ def declare(lib) -> None:
     _proto(lib, "lx_sim_counters", C.c_int, sim, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64))
     _proto(lib, "lx_hdf5_write", C.c_int, C.c_char_p, C.c_int, P(C.c_char_p), P(P(C.c_double)), P(C.c_int))
     _proto(lib, "lx_hdf5_read", C.c_int, C.c_char_p, C.c_char_p, P(C.c_double), C.c_size_t, P(C.c_int))
+    _proto(lib, "lx_batch_create", C.c_int, P(C.c_void_p))
+    _proto(lib, "lx_batch_destroy", None, C.c_void_p)
+    _proto(lib, "lx_batch_add", C.c_int, C.c_void_p, sim)
+    _proto(lib, "lx_batch_remove", C.c_int, C.c_void_p, sim)
+    _proto(lib, "lx_batch_size", C.c_int, C.c_void_p)
+    _proto(lib, "lx_batch_set_chunk", C.c_int, C.c_void_p, C.c_int)
+    _proto(lib, "lx_batch_step", C.c_int, C.c_void_p, C.c_int)
     _proto(lib, "lx_host_alloc", C.c_int, C.c_size_t, P(C.c_void_p))
     _proto(lib, "lx_host_free", None, C.c_void_p)
     _proto(lib, "lx_last_error", C.c_char_p, sim)

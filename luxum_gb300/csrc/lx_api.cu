@@ -1023,9 +1023,7 @@ struct KernelTimer {
   int cnt[4] = {0, 0, 0, 0};
 };
 
-template <class T, class C>
-static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
-  lx::StepParams<T, C> sp = step_params<T, C>(s);
+static lx::PrologueParams make_prologue(lx_sim* s) {
   lx::PrologueParams pp;
   std::memset(&pp, 0, sizeof pp);
   pp.nsets = 12;
@@ -1035,7 +1033,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
       pp.sets[6 + c * 2 + q] = s->setsE[c][q];
     }
   pp.tab = s->tab;
-  pp.tab_total = sp.tfsf ? s->tab_total : 0;
+  pp.tab_total = (s->tfsf && s->tab_total > 0) ? s->tab_total : 0;
   pp.planar = s->planar;
   pp.dx = s->k.dx; pp.dy = s->k.dy; pp.dz = s->k.dz;
   pp.kx = s->k.k[0]; pp.ky = s->k.k[1]; pp.kz = s->k.k[2];
@@ -1051,6 +1049,13 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
   pp.src_t0 = s->p.src_t0;
   pp.src_tw = s->p.src_tw;
   pp.prec = s->prec;
+  return pp;
+}
+
+template <class T, class C>
+static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
+  lx::StepParams<T, C> sp = step_params<T, C>(s);
+  lx::PrologueParams pp = make_prologue(s);
   T* pf[6] = {(T*)s->E[0], (T*)s->E[1], (T*)s->E[2], (T*)s->H[0], (T*)s->H[1], (T*)s->H[2]};
   lx::ProbeParams prb;
   std::memset(&prb, 0, sizeof prb);
@@ -1237,4 +1242,289 @@ extern "C" LX_API lx_status lx_host_alloc(size_t bytes, void** ptr) {
 
 extern "C" LX_API void lx_host_free(void* ptr) {
   if (ptr) cudaFreeHost(ptr);
+}
+
+// ------------------------------------------------------------------ batches
+
+struct lx_batch {
+  std::vector<lx_sim*> sims;
+  int prec = -1;
+  int chunk = 100;
+  bool dirty = true;
+  cudaStream_t stream = nullptr;
+  struct Group {
+    bool planar = false, uniform = false;
+    std::vector<int> members;  // batch-global indices
+    void* d_params = nullptr;
+    lx::Tile* d_tiles = nullptr;
+    int ntiles = 0;
+  };
+  std::vector<Group> groups;
+  lx::PrologueParams* d_pps = nullptr;
+  int max_entries = 0;
+  bool need_prologue = false;
+  int* d_ts = nullptr;
+  unsigned long long* d_slots = nullptr;
+  lx::DftParams* d_dfts = nullptr;
+  int ndft = 0;
+  long long max_cells4 = 0;
+  cudaGraphExec_t exec = nullptr;
+  int exec_steps = 0;
+  std::vector<int> host_ts;
+  std::string err;
+};
+
+static void batch_free_device(lx_batch* b) {
+  for (auto& g : b->groups) {
+    cudaFree(g.d_params);
+    cudaFree(g.d_tiles);
+  }
+  b->groups.clear();
+  cudaFree(b->d_pps);
+  cudaFree(b->d_ts);
+  cudaFree(b->d_slots);
+  cudaFree(b->d_dfts);
+  b->d_pps = nullptr;
+  b->d_ts = nullptr;
+  b->d_slots = nullptr;
+  b->d_dfts = nullptr;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  b->exec_steps = 0;
+}
+
+static lx_status bfail(lx_batch* b, lx_status st, const std::string& m) {
+  if (b) b->err = m;
+  return fail(nullptr, st, m);
+}
+
+#define BCK(...)                                                                                      \
+  do {                                                                                                \
+    cudaError_t e_ = (__VA_ARGS__);                                                                   \
+    if (e_ != cudaSuccess) return bfail(b, e_ == cudaErrorMemoryAllocation ? LX_ERR_OOM : LX_ERR_CUDA, \
+                                        std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+extern "C" LX_API lx_status lx_batch_create(lx_batch** out) {
+  if (!out) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  lx_batch* b = new (std::nothrow) lx_batch();
+  if (!b) return fail(nullptr, LX_ERR_OOM, "host allocation failed");
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete b;
+    return fail(nullptr, LX_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+  }
+  *out = b;
+  return LX_OK;
+}
+
+extern "C" LX_API void lx_batch_destroy(lx_batch* b) {
+  if (!b) return;
+  cudaStreamSynchronize(b->stream);
+  batch_free_device(b);
+  cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+extern "C" LX_API int lx_batch_size(const lx_batch* b) { return b ? (int)b->sims.size() : 0; }
+
+extern "C" LX_API lx_status lx_batch_set_chunk(lx_batch* b, int steps) {
+  if (!b || steps < 0) return fail(nullptr, LX_ERR_INVALID, "chunk must be >= 0");
+  b->chunk = steps;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  b->exec_steps = 0;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_batch_add(lx_batch* b, lx_sim* s) {
+  if (!b || !s) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  for (auto* m : b->sims)
+    if (m == s) return bfail(b, LX_ERR_INVALID, "handle already in this batch");
+  if (b->prec >= 0 && s->prec != b->prec) return bfail(b, LX_ERR_INVALID, "all members of a batch share one precision");
+  if (!s->outputs.empty() || s->nprobes > 0)
+    return bfail(b, LX_ERR_UNSUPPORTED, "batched members cannot have snapshot outputs or probes");
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  b->prec = s->prec;
+  b->sims.push_back(s);
+  b->dirty = true;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_batch_remove(lx_batch* b, lx_sim* s) {
+  if (!b || !s) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  for (size_t q = 0; q < b->sims.size(); q++)
+    if (b->sims[q] == s) {
+      BCK(cudaStreamSynchronize(b->stream));
+      b->sims.erase(b->sims.begin() + q);
+      b->dirty = true;
+      if (b->sims.empty()) b->prec = -1;
+      return LX_OK;
+    }
+  return bfail(b, LX_ERR_INVALID, "handle is not in this batch");
+}
+
+template <class T, class C>
+static lx_status batch_rebuild(lx_batch* b) {
+  BCK(cudaStreamSynchronize(b->stream));
+  batch_free_device(b);
+  const int n = (int)b->sims.size();
+  std::vector<lx::PrologueParams> pps(n);
+  std::vector<lx::DftParams> dfts;
+  b->max_entries = 0;
+  b->need_prologue = false;
+  b->max_cells4 = 0;
+  b->host_ts.resize(n);
+  BCK(cudaMalloc(&b->d_slots, sizeof(unsigned long long) * (n > 0 ? n : 1)));
+  for (int q = 0; q < n; q++) {
+    lx_sim* s = b->sims[q];
+    pps[q] = make_prologue(s);
+    pps[q].max_slot = b->d_slots + q;
+    b->max_entries = std::max(b->max_entries, pps[q].tab_total);
+    b->host_ts[q] = s->t;
+    T* pf[6] = {(T*)s->E[0], (T*)s->E[1], (T*)s->E[2], (T*)s->H[0], (T*)s->H[1], (T*)s->H[2]};
+    for (auto& d : s->dfts) {
+      lx::DftParams dp;
+      std::memset(&dp, 0, sizeof dp);
+      dp.axis = d.axis; dp.index = d.index; dp.na = d.na; dp.nb = d.nb; dp.Ny = s->Ny; dp.Nzp = s->Nzp;
+      dp.nfreq = d.nfreq; dp.dt = s->k.dt; dp.weight = (double)d.every; dp.every_ = d.every;
+      dp.omega = d.d_omega; dp.acc = d.d_acc; dp.sim = q;
+      for (int c = 0; c < 4; c++) {
+        dp.f[c] = pf[d.comps[c]];
+        for (int a = 0; a < 3; a++) dp.ext[c][a] = s->ext[d.comps[c]][a];
+      }
+      dfts.push_back(dp);
+      b->max_cells4 = std::max(b->max_cells4, 4LL * d.na * d.nb);
+    }
+    // groups by (planar, uniform)
+    int gi = -1;
+    for (size_t g = 0; g < b->groups.size(); g++)
+      if (b->groups[g].planar == (bool)s->planar && b->groups[g].uniform == (bool)s->uniform) gi = (int)g;
+    if (gi < 0) {
+      b->groups.emplace_back();
+      b->groups.back().planar = s->planar;
+      b->groups.back().uniform = s->uniform;
+      gi = (int)b->groups.size() - 1;
+    }
+    b->groups[gi].members.push_back(q);
+  }
+  b->need_prologue = n > 0;  // monitor slots are reset every step
+  BCK(cudaMalloc(&b->d_pps, sizeof(lx::PrologueParams) * (n > 0 ? n : 1)));
+  BCK(cudaMemcpy(b->d_pps, pps.data(), sizeof(lx::PrologueParams) * n, cudaMemcpyHostToDevice));
+  BCK(cudaMalloc(&b->d_ts, sizeof(int) * (n > 0 ? n : 1)));
+  BCK(cudaMemcpy(b->d_ts, b->host_ts.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  b->ndft = (int)dfts.size();
+  if (b->ndft) {
+    BCK(cudaMalloc(&b->d_dfts, sizeof(lx::DftParams) * b->ndft));
+    BCK(cudaMemcpy(b->d_dfts, dfts.data(), sizeof(lx::DftParams) * b->ndft, cudaMemcpyHostToDevice));
+  }
+  for (auto& g : b->groups) {
+    std::vector<lx::StepParams<T, C>> ps;
+    std::vector<lx::Tile> tiles;
+    for (size_t li = 0; li < g.members.size(); li++) {
+      lx_sim* s = b->sims[g.members[li]];
+      lx::StepParams<T, C> sp = step_params<T, C>(s);
+      sp.max_slot = b->d_slots + g.members[li];
+      sp.etotal = nullptr;
+      ps.push_back(sp);
+      if (s->planar) {
+        for (int i0 = 0; i0 < s->Nx; i0 += 8)
+          for (int k0 = 0; k0 < s->Nz; k0 += 32) tiles.push_back({(int)li, i0, 0, k0});
+      } else {
+        for (int i = 0; i < s->Nx; i++)
+          for (int j0 = 0; j0 < s->Ny; j0 += 8)
+            for (int k0 = 0; k0 < s->Nz; k0 += 32) tiles.push_back({(int)li, i, j0, k0});
+      }
+    }
+    if ((long long)tiles.size() > 0x7fffffffLL) return bfail(b, LX_ERR_INVALID, "batch too large for one launch");
+    g.ntiles = (int)tiles.size();
+    BCK(cudaMalloc(&g.d_params, sizeof(lx::StepParams<T, C>) * ps.size()));
+    BCK(cudaMemcpy(g.d_params, ps.data(), sizeof(lx::StepParams<T, C>) * ps.size(), cudaMemcpyHostToDevice));
+    BCK(cudaMalloc(&g.d_tiles, sizeof(lx::Tile) * (tiles.empty() ? 1 : tiles.size())));
+    BCK(cudaMemcpy(g.d_tiles, tiles.data(), sizeof(lx::Tile) * tiles.size(), cudaMemcpyHostToDevice));
+  }
+  b->dirty = false;
+  return LX_OK;
+}
+
+template <class T, class C>
+static lx_status batch_enqueue(lx_batch* b, int nsteps) {
+  const int n = (int)b->sims.size();
+  for (int q = 0; q < nsteps; q++) {
+    if (b->need_prologue) BCK(lx::launch_prologue_batch<C>(b->d_pps, b->d_ts, n, b->max_entries, b->stream));
+    for (auto& g : b->groups)
+      BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.ntiles, g.planar, g.uniform,
+                                      true, b->stream));
+    for (auto& g : b->groups)
+      BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.ntiles, g.planar, g.uniform,
+                                      false, b->stream));
+    if (b->ndft) BCK(lx::launch_dft_batch<T>(b->d_dfts, b->ndft, b->max_cells4, b->d_ts, b->stream));
+    BCK(lx::launch_tick(b->d_ts, n, b->stream));
+  }
+  return LX_OK;
+}
+
+template <class T, class C>
+static lx_status batch_run(lx_batch* b, int nsteps) {
+  lx_status st;
+  // a member stepped on its own since the last batch step -> re-read step counters
+  bool moved = false;
+  for (size_t q = 0; q < b->sims.size() && !b->dirty; q++) moved |= (b->sims[q]->t != b->host_ts[q]);
+  if (b->dirty) {
+    if ((st = batch_rebuild<T, C>(b))) return st;
+  } else if (moved) {
+    for (size_t q = 0; q < b->sims.size(); q++) b->host_ts[q] = b->sims[q]->t;
+    BCK(cudaMemcpyAsync(b->d_ts, b->host_ts.data(), sizeof(int) * b->sims.size(), cudaMemcpyHostToDevice, b->stream));
+  }
+  for (auto* s : b->sims) BCK(cudaStreamSynchronize(s->stream));  // members' own pending work first
+  int done = 0;
+  if (b->chunk > 0) {
+    while (nsteps - done >= b->chunk) {
+      if (!b->exec || b->exec_steps != b->chunk) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+        cudaGraph_t g;
+        BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        st = batch_enqueue<T, C>(b, b->chunk);
+        cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+        if (st) return st;
+        BCK(ce);
+        ce = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        BCK(ce);
+        b->exec_steps = b->chunk;
+      }
+      BCK(cudaGraphLaunch(b->exec, b->stream));
+      done += b->chunk;
+    }
+  }
+  if (nsteps - done > 0) {
+    if ((st = batch_enqueue<T, C>(b, nsteps - done))) return st;
+  }
+  const int n = (int)b->sims.size();
+  std::vector<unsigned long long> slots(n);
+  if (n) BCK(cudaMemcpyAsync(slots.data(), b->d_slots, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  std::string bad;
+  for (int q = 0; q < n; q++) {
+    lx_sim* s = b->sims[q];
+    s->t += nsteps;
+    b->host_ts[q] = s->t;
+    s->n_kernels += (uint64_t)nsteps * 4;
+    double v;
+    std::memcpy(&v, &slots[q], sizeof v);
+    s->last_max = v;
+    if (!std::isfinite(v) && bad.empty()) bad = "member " + std::to_string(q) + ": max|E|^2 is not finite";
+  }
+  if (!bad.empty()) return bfail(b, LX_ERR_BLOWUP, bad);
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_batch_step(lx_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return fail(nullptr, LX_ERR_INVALID, "bad argument");
+  if (b->sims.empty() || nsteps == 0) return LX_OK;
+  if (b->prec == LX_PREC_FP64) return batch_run<double, double>(b, nsteps);
+  if (b->prec == LX_PREC_FP32) return batch_run<float, float>(b, nsteps);
+  return batch_run<__half, float>(b, nsteps);
 }

@@ -116,11 +116,22 @@ struct ProbeParams {
   const int* ijk;   // device array [nprobes][3]
 };
 
+// One tile of a batched launch: 32 (z) x 8 (y, or x in planar grids) cells of one simulation.
+struct Tile {
+  int sim;  // index into the batch's parameter array
+  int a;    // 3-D: x plane; planar: first x index
+  int b;    // 3-D: first y index
+  int c;    // first z index
+};
+
 // One DFT plane monitor (see lx_sim_add_dft_plane).
 struct DftParams {
   int axis, index, na, nb, Ny, Nzp, nfreq, t;
+  int sim;                // batched launches: index of the simulation's step counter
+  const void* f[4];       // batched launches: the four sampled components
   int ext[4][3];          // extents of the four sampled components
   double dt, weight;
+  int every_;             // batched launches: sampling cadence
   const double* omega;    // device [nfreq]
   double* acc;            // device [nfreq][4][na*nb][2]
 };

@@ -50,19 +50,17 @@ __device__ __forceinline__ float fmaC(float a, float b, float c) { return fmaf(a
 template <class C>
 __device__ __forceinline__ void tfsf_apply(const PatchSet& ps, const C* tab, int i, int j, int k, C& d) {
   if (!ps.active) return;
-  const int u[3] = {i, j, k};
   const int a = ps.axis;
-  const int n = u[a];
+  const int n = a == 0 ? i : (a == 1 ? j : k);
   const bool h0 = (n == ps.plane[0]);
   const bool h1 = (n == ps.plane[1]);
   if (!(h0 || h1)) return;
-  int off = 0;
-#pragma unroll
-  for (int b = 0; b < 3; ++b) {
-    if (b == a) continue;
-    if (u[b] < ps.lo[b] || u[b] > ps.hi[b]) return;
-    off += (u[b] - ps.lo[b]) * ps.stride[b];
-  }
+  // in-plane ranges and table offset (the normal axis has lo = hi = 0 and stride 0 in the
+  // checks below, so it is excluded by selecting 0 for it)
+  const int ui = a == 0 ? 0 : i - ps.lo[0], uj = a == 1 ? 0 : j - ps.lo[1], uk = a == 2 ? 0 : k - ps.lo[2];
+  const int wi = a == 0 ? 0 : ps.hi[0] - ps.lo[0], wj = a == 1 ? 0 : ps.hi[1] - ps.lo[1], wk = a == 2 ? 0 : ps.hi[2] - ps.lo[2];
+  if (ui < 0 || uj < 0 || uk < 0 || ui > wi || uj > wj || uk > wk) return;
+  const int off = ui * ps.stride[0] + uj * ps.stride[1] + uk * ps.stride[2];
   if (h0) d = d + tab[ps.tab + off];
   if (h1) d = d + tab[ps.tab + ps.plane_len + off];
 }
@@ -84,7 +82,7 @@ __device__ __forceinline__ long long psi_index(int axis, const Slab& s, int si_,
 
 // ------------------------------------------------------------------ prologue
 
-__device__ double incident_value(const PrologueParams& p, const PatchSet& ps, int plane, int e) {
+__device__ double incident_value(const PrologueParams& p, const PatchSet& ps, int plane, int e, int t) {
   // table entry e of `plane` -> in-plane indices -> wave positions
   double pos[3];
   int rem = e;
@@ -107,7 +105,7 @@ __device__ double incident_value(const PrologueParams& p, const PatchSet& ps, in
   else
     X = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(pos[0], p.dx), p.kx), __dmul_rn(__dmul_rn(pos[1], p.dy), p.ky)),
                   __dmul_rn(__dmul_rn(pos[2], p.dz), p.kz));
-  const double tt = ps.hcurl ? (double)p.t : (double)p.t - 0.5;
+  const double tt = ps.hcurl ? (double)t : (double)t - 0.5;
   X = __dsub_rn(__dadd_rn(X, __dmul_rn(p.init, p.dx)), __dmul_rn(__dmul_rn(tt, p.c), p.dt));
   double v = exp(__ddiv_rn(-__dmul_rn(X, X), p.pw_sigma));
   v = __dmul_rn(v, ps.neg);
@@ -119,20 +117,20 @@ __device__ double incident_value(const PrologueParams& p, const PatchSet& ps, in
 }
 
 template <class C>
-__global__ void prologue_kernel(const PrologueParams p, C* tab_out) {
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void prologue_body(const PrologueParams& p, const int t, C* tab_out, const int gid,
+                                              const int gstride) {
   if (gid == 0) {
     if (p.max_slot) *p.max_slot = 0ull;
     if (p.src_kind == 0) {
       // amp_source*sin(omega_source*t*dt), int members (maxwell.h:203,206; three_dim_pml.cc:163)
-      const int wt = (int)((unsigned)p.src_omega_i * (unsigned)p.t);
+      const int wt = (int)((unsigned)p.src_omega_i * (unsigned)t);
       const double v = (double)p.src_amp_i * sin((double)wt * p.dt);
       if (p.prec == 0) ((double*)p.src_field)[p.src_idx] = v;
       else if (p.prec == 1) ((float*)p.src_field)[p.src_idx] = (float)v;
       else ((__half*)p.src_field)[p.src_idx] = __double2half(v);
     } else if (p.src_kind == 1) {
-      const double u = (p.t - p.src_t0) / p.src_tw;
-      const double v = p.src_amp * exp(-(u * u)) * sin(p.src_omega * p.t * p.dt);
+      const double u = (t - p.src_t0) / p.src_tw;
+      const double v = p.src_amp * exp(-(u * u)) * sin(p.src_omega * t * p.dt);
       if (p.prec == 0) ((double*)p.src_field)[p.src_idx] += v;
       else if (p.prec == 1) ((float*)p.src_field)[p.src_idx] += (float)v;
       else {
@@ -141,7 +139,7 @@ __global__ void prologue_kernel(const PrologueParams p, C* tab_out) {
       }
     }
   }
-  for (int e = gid; e < p.tab_total; e += gridDim.x * blockDim.x) {
+  for (int e = gid; e < p.tab_total; e += gstride) {
     int rem = e;
     for (int s = 0; s < p.nsets; ++s) {
       const PatchSet& ps = p.sets[s];
@@ -149,13 +147,31 @@ __global__ void prologue_kernel(const PrologueParams p, C* tab_out) {
       const int len = 2 * ps.plane_len;
       if (rem < len) {
         const int plane = rem >= ps.plane_len ? 1 : 0;
-        const double v = incident_value(p, ps, plane, rem - plane * ps.plane_len);
+        const double v = incident_value(p, ps, plane, rem - plane * ps.plane_len, t);
         tab_out[ps.tab + rem] = (C)v;
         break;
       }
       rem -= len;
     }
   }
+}
+
+template <class C>
+__global__ void prologue_kernel(const PrologueParams p, C* tab_out) {
+  prologue_body<C>(p, p.t, tab_out, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// Batched prologue: blockIdx.y selects the simulation; its step counter lives on the device
+// so that a captured chunk of steps can be replayed.
+template <class C>
+__global__ void prologue_batch_kernel(const PrologueParams* __restrict__ pps, const int* __restrict__ ts) {
+  const PrologueParams& p = pps[blockIdx.y];
+  prologue_body<C>(p, ts[blockIdx.y], (C*)p.tab, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+__global__ void tick_kernel(int* ts, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) ts[s] += 1;
 }
 
 // ------------------------------------------------------------------ monitor
@@ -191,11 +207,7 @@ __device__ __forceinline__ unsigned long long e2_bits(float v) {
 
 // H half-step over cell (i,j,k) for Hx, Hy, Hz (three_dim_pml.cc:176-213, three_dim.cc:101-132).
 template <class T, class C, bool UNI>
-__global__ void __launch_bounds__(256) h_kernel_3d(const StepParams<T, C> p) {
-  const int k = blockIdx.x * 32 + threadIdx.x;
-  const int j = blockIdx.y * 8 + threadIdx.y;
-  const int i = blockIdx.z;
-  if (k >= p.Nz || j >= p.Ny) return;
+__device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k) {
   const long long c = (long long)i * p.si + (long long)j * p.sj + k;
   const C ex = ld<T, C>(p.E[0] + c), ey = ld<T, C>(p.E[1] + c), ez = ld<T, C>(p.E[2] + c);
   int sx = -1, sy = -1, sz = -1;
@@ -248,17 +260,22 @@ __global__ void __launch_bounds__(256) h_kernel_3d(const StepParams<T, C> p) {
   }
 }
 
-// E half-step over cell (i,j,k) for Ex, Ey, Ez (three_dim_pml.cc:218-276, three_dim.cc:134-189).
-// Only cells where the reference's H-curl is computed (vfield.cc:241-269: the transverse
-// index in [1, N-2]) change; on the PEC walls the reference adds Cb*0 and psi stays 0.
 template <class T, class C, bool UNI>
-__global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
+__global__ void __launch_bounds__(256) h_kernel_3d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
   const int i = blockIdx.z;
-  const bool in = (k < p.Nz && j < p.Ny);
+  if (k < p.Nz && j < p.Ny) h_cell_3d<T, C, UNI>(p, i, j, k);
+}
+
+// E half-step over cell (i,j,k) for Ex, Ey, Ez (three_dim_pml.cc:218-276, three_dim.cc:134-189).
+// Only cells where the reference's H-curl is computed (vfield.cc:241-269: the transverse
+// index in [1, N-2]) change; on the PEC walls the reference adds Cb*0 and psi stays 0.
+// Returns the bit pattern of this cell's |E|^2 when monitoring (0 otherwise).
+template <class T, class C, bool UNI>
+__device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k) {
   unsigned long long mbits = 0ull;
-  if (in) {
+  {
     const long long c = (long long)i * p.si + (long long)j * p.sj + k;
     const C hx = ld<T, C>(p.H[0] + c), hy = ld<T, C>(p.H[1] + c), hz = ld<T, C>(p.H[2] + c);
     int sx = -1, sy = -1, sz = -1;
@@ -325,6 +342,15 @@ __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
       mbits = e2_bits(e2);
     }
   }
+  return mbits;
+}
+
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int i = blockIdx.z;
+  const unsigned long long mbits = (k < p.Nz && j < p.Ny) ? e_cell_3d<T, C, UNI>(p, i, j, k) : 0ull;
   if (p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
@@ -332,10 +358,7 @@ __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
 
 // Planar H half-step (x-z plane, Ny = 1): Hx and Hz (two_dim_pml.cc:144-162, two_dim.cc:95-111).
 template <class T, class C, bool UNI>
-__global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
-  const int k = blockIdx.x * 32 + threadIdx.x;
-  const int i = blockIdx.y * 8 + threadIdx.y;
-  if (k >= p.Nz || i >= p.Nx) return;
+__device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i, const int k) {
   const long long c = (long long)i * p.si + k;
   const C ey = ld<T, C>(p.E[1] + c);
   // Hx: k < Nz-1; Hx -= Db*(-curl2/kappa - psi2), curl2 = dEy/dz (z profile)
@@ -362,15 +385,20 @@ __global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
   }
 }
 
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int i = blockIdx.y * 8 + threadIdx.y;
+  if (k < p.Nz && i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k);
+}
+
 // Planar E half-step: Ey (two_dim_pml.cc:164-181, two_dim.cc:113-128).  The reference loop
 // covers i < Nx-1, k < Nz-1, but its H-curl is only computed for i, k in [1, N-2]
 // (vfield.cc:376-381), so the other cells add Cb*0 and are skipped here.
 template <class T, class C, bool UNI>
-__global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
-  const int k = blockIdx.x * 32 + threadIdx.x;
-  const int i = blockIdx.y * 8 + threadIdx.y;
+__device__ __forceinline__ unsigned long long e_cell_2d(const StepParams<T, C>& p, const int i, const int k) {
   unsigned long long mbits = 0ull;
-  if (k < p.Nz && i < p.Nx) {
+  {
     const long long c = (long long)i * p.si + k;
     C eyn;
     if (i >= 1 && i < p.Nx - 1 && k >= 1 && k < p.Nz - 1) {
@@ -394,6 +422,51 @@ __global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
     // local_max = max(Ey*Ey) over the whole Ey array (two_dim_pml.cc:181)
     if (p.max_slot) mbits = e2_bits(eyn * eyn);
   }
+  return mbits;
+}
+
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int i = blockIdx.y * 8 + threadIdx.y;
+  const unsigned long long mbits = (k < p.Nz && i < p.Nx) ? e_cell_2d<T, C, UNI>(p, i, k) : 0ull;
+  if (p.max_slot) block_max_atomic(mbits, p.max_slot);
+}
+
+// ------------------------------------------------------------------ batched update kernels
+
+// One block per tile of one simulation of the batch; the parameters come from global memory.
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) h_batch_3d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
+  const Tile tl = tiles[blockIdx.x];
+  const StepParams<T, C>& p = ps[tl.sim];
+  const int k = tl.c + threadIdx.x, j = tl.b + threadIdx.y, i = tl.a;
+  if (k < p.Nz && j < p.Ny) h_cell_3d<T, C, UNI>(p, i, j, k);
+}
+
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
+  const Tile tl = tiles[blockIdx.x];
+  const StepParams<T, C>& p = ps[tl.sim];
+  const int k = tl.c + threadIdx.x, j = tl.b + threadIdx.y, i = tl.a;
+  const unsigned long long mbits = (k < p.Nz && j < p.Ny) ? e_cell_3d<T, C, UNI>(p, i, j, k) : 0ull;
+  if (p.max_slot) block_max_atomic(mbits, p.max_slot);
+}
+
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
+  const Tile tl = tiles[blockIdx.x];
+  const StepParams<T, C>& p = ps[tl.sim];
+  const int k = tl.c + threadIdx.x, i = tl.a + threadIdx.y;
+  if (k < p.Nz && i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k);
+}
+
+template <class T, class C, bool UNI>
+__global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
+  const Tile tl = tiles[blockIdx.x];
+  const StepParams<T, C>& p = ps[tl.sim];
+  const int k = tl.c + threadIdx.x, i = tl.a + threadIdx.y;
+  const unsigned long long mbits = (k < p.Nz && i < p.Nx) ? e_cell_2d<T, C, UNI>(p, i, k) : 0ull;
   if (p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
@@ -488,11 +561,12 @@ __global__ void probe_kernel(const ProbeParams pp, const T* f0, const T* f1, con
 // phase factors of every frequency once into shared memory; each thread owns one
 // (component, cell) and updates its nfreq complex accumulators (coalesced along the cell).
 template <class T>
-__global__ void dft_kernel(const DftParams d, const T* f0, const T* f1, const T* f2, const T* f3) {
+__device__ __forceinline__ void dft_body(const DftParams& d, const int t, const T* f0, const T* f1, const T* f2,
+                                         const T* f3) {
   __shared__ double cs[2][kMaxDftFreq], sn[2][kMaxDftFreq];
   for (int f = threadIdx.x; f < d.nfreq; f += blockDim.x) {
-    const double pe = __dmul_rn(d.omega[f], __dmul_rn((double)(d.t + 1), d.dt));
-    const double ph = __dmul_rn(d.omega[f], __dmul_rn((double)d.t + 0.5, d.dt));
+    const double pe = __dmul_rn(d.omega[f], __dmul_rn((double)(t + 1), d.dt));
+    const double ph = __dmul_rn(d.omega[f], __dmul_rn((double)t + 0.5, d.dt));
     sincos(pe, &sn[0][f], &cs[0][f]);
     sincos(ph, &sn[1][f], &cs[1][f]);
   }
@@ -523,6 +597,22 @@ __global__ void dft_kernel(const DftParams d, const T* f0, const T* f1, const T*
     x.y = fma(-v, sn[w][fq], x.y);
     acc[((long long)fq * 4 + comp) * ncell + cell] = x;
   }
+}
+
+template <class T>
+__global__ void dft_kernel(const DftParams d, const T* f0, const T* f1, const T* f2, const T* f3) {
+  dft_body<T>(d, d.t, f0, f1, f2, f3);
+}
+
+// Batched DFT planes: blockIdx.y selects the plane; sampled when the owner's step counter
+// (before this step's tick) is a multiple of the plane's cadence.
+template <class T>
+__global__ void dft_batch_kernel(const DftParams* __restrict__ ds, const int* __restrict__ ts) {
+  const DftParams& d = ds[blockIdx.y];
+  const int t = ts[d.sim];
+  if (t % d.every_ != 0) return;
+  if ((long long)blockIdx.x * blockDim.x >= 4LL * d.na * d.nb) return;
+  dft_body<T>(d, t, (const T*)d.f[0], (const T*)d.f[1], (const T*)d.f[2], (const T*)d.f[3]);
 }
 
 // ------------------------------------------------------------------ launchers
@@ -604,18 +694,71 @@ cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <class T, class C>
+cudaError_t launch_batch_step(const StepParams<T, C>* ps, const Tile* tiles, int ntiles, bool planar, bool uniform,
+                              bool h_half, cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  dim3 block(32, 8);
+  if (planar) {
+    if (h_half) {
+      if (uniform) h_batch_2d<T, C, true><<<ntiles, block, 0, s>>>(ps, tiles);
+      else h_batch_2d<T, C, false><<<ntiles, block, 0, s>>>(ps, tiles);
+    } else {
+      if (uniform) e_batch_2d<T, C, true><<<ntiles, block, 0, s>>>(ps, tiles);
+      else e_batch_2d<T, C, false><<<ntiles, block, 0, s>>>(ps, tiles);
+    }
+  } else {
+    if (h_half) {
+      if (uniform) h_batch_3d<T, C, true><<<ntiles, block, 0, s>>>(ps, tiles);
+      else h_batch_3d<T, C, false><<<ntiles, block, 0, s>>>(ps, tiles);
+    } else {
+      if (uniform) e_batch_3d<T, C, true><<<ntiles, block, 0, s>>>(ps, tiles);
+      else e_batch_3d<T, C, false><<<ntiles, block, 0, s>>>(ps, tiles);
+    }
+  }
+  return cudaGetLastError();
+}
+
+template <class C>
+cudaError_t launch_prologue_batch(const PrologueParams* pps, const int* ts, int nsims, int max_entries, cudaStream_t s) {
+  if (nsims <= 0) return cudaSuccess;
+  long long gx = (max_entries + 255) / 256;
+  if (gx < 1) gx = 1;
+  if (gx > 1024) gx = 1024;
+  prologue_batch_kernel<C><<<dim3((unsigned)gx, (unsigned)nsims), 256, 0, s>>>(pps, ts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tick(int* ts, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  tick_kernel<<<(n + 255) / 256, 256, 0, s>>>(ts, n);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_dft_batch(const DftParams* ds, int nplanes, long long max_cells4, const int* ts, cudaStream_t s) {
+  if (nplanes <= 0) return cudaSuccess;
+  dft_batch_kernel<T><<<dim3((unsigned)((max_cells4 + 255) / 256), (unsigned)nplanes), 256, 0, s>>>(ds, ts);
+  return cudaGetLastError();
+}
+
 #define LX_INST(T, C)                                                                                                  \
   template cudaError_t launch_step<T, C>(const StepParams<T, C>&, bool, bool, bool, cudaStream_t);                   \
   template cudaError_t launch_gather<T>(const T*, double*, const int[3], int, int, cudaStream_t);                     \
   template cudaError_t launch_scatter<T>(const double*, T*, const int[3], int, int, int, double, double, double,      \
                                          double, cudaStream_t);                                                        \
   template cudaError_t launch_probes<T>(const ProbeParams&, T* const[6], double*, cudaStream_t);                   \
-  template cudaError_t launch_dft<T>(const DftParams&, T* const[4], cudaStream_t);
+  template cudaError_t launch_dft<T>(const DftParams&, T* const[4], cudaStream_t);                                 \
+  template cudaError_t launch_batch_step<T, C>(const StepParams<T, C>*, const Tile*, int, bool, bool, bool,         \
+                                               cudaStream_t);                                                          \
+  template cudaError_t launch_dft_batch<T>(const DftParams*, int, long long, const int*, cudaStream_t);
 LX_INST(double, double)
 LX_INST(float, float)
 LX_INST(__half, float)
 template cudaError_t launch_prologue<double>(const PrologueParams&, cudaStream_t);
 template cudaError_t launch_prologue<float>(const PrologueParams&, cudaStream_t);
+template cudaError_t launch_prologue_batch<double>(const PrologueParams*, const int*, int, int, cudaStream_t);
+template cudaError_t launch_prologue_batch<float>(const PrologueParams*, const int*, int, int, cudaStream_t);
 template cudaError_t launch_eps_box<double>(double*, const int[3], int, int, const int[3], const int[3], double,
                                             cudaStream_t);
 template cudaError_t launch_eps_box<float>(float*, const int[3], int, int, const int[3], const int[3], double,

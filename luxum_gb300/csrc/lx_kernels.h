@@ -24,4 +24,13 @@ cudaError_t launch_probes(const ProbeParams& pp, T* const f[6], double* out, cud
 template <class T>
 cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s);
 
+template <class T, class C>
+cudaError_t launch_batch_step(const StepParams<T, C>* ps, const Tile* tiles, int ntiles, bool planar, bool uniform,
+                              bool h_half, cudaStream_t s);
+template <class C>
+cudaError_t launch_prologue_batch(const PrologueParams* pps, const int* ts, int nsims, int max_entries, cudaStream_t s);
+cudaError_t launch_tick(int* ts, int n, cudaStream_t s);
+template <class T>
+cudaError_t launch_dft_batch(const DftParams* ds, int nplanes, long long max_cells4, const int* ts, cudaStream_t s);
+
 }  // namespace lx

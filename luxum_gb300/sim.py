@@ -235,3 +235,46 @@ def hdf5_read(path: str, dataset: str) -> np.ndarray:
     if st:
         raise LuxumError(st, lib.lx_last_error(None).decode())
     return out
+
+
+class Batch:
+    """Many simulations stepped together (lx_batch_*): one launch per half step for all."""
+
+    def __init__(self, chunk: int = 100):
+        self.lib = _ffi.lib()
+        h = C.c_void_p()
+        st = self.lib.lx_batch_create(C.byref(h))
+        if st:
+            raise LuxumError(st, self.lib.lx_last_error(None).decode())
+        self.h = h
+        self.members = []
+        self._check(self.lib.lx_batch_set_chunk(self.h, chunk))
+
+    def _check(self, st: int) -> None:
+        if st:
+            raise LuxumError(st, self.lib.lx_last_error(None).decode())
+
+    def add(self, sim: Sim) -> None:
+        self._check(self.lib.lx_batch_add(self.h, sim.h))
+        self.members.append(sim)
+
+    def remove(self, sim: Sim) -> None:
+        self._check(self.lib.lx_batch_remove(self.h, sim.h))
+        self.members.remove(sim)
+
+    def step(self, n: int) -> None:
+        self._check(self.lib.lx_batch_step(self.h, n))
+
+    def __len__(self):
+        return self.lib.lx_batch_size(self.h)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.lx_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
