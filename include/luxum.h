@@ -156,6 +156,20 @@ LX_API lx_status lx_sim_sync(lx_sim* sim);
 LX_API lx_status lx_sim_field_shape(const lx_sim* sim, int comp, int shape[3]);
 LX_API lx_status lx_sim_read_field(lx_sim* sim, int comp, double* host, size_t n);
 LX_API lx_status lx_sim_write_field(lx_sim* sim, int comp, const double* host, size_t n);
+/* Same result as lx_sim_read_field, but the call allocates nothing: no cudaMalloc, cudaFree
+ * or allocating library routine.  No counterpart in the reference.  It is meant for callers
+ * that must not let a library allocate device memory at that point: processes whose GPU
+ * memory is owned by another allocator (a framework caching allocator that has reserved
+ * most of the device, where a new cudaMalloc fails or fragments its pool) and loops with
+ * latency budgets (cudaMalloc/cudaFree can synchronise the device).  The component is
+ * compacted through a fixed staging array of 1048576 doubles (8 MiB) that is part of the
+ * library's static device memory; every GPU that loads the library holds it until the
+ * process exits.  Components with more values than that are rejected with LX_ERR_INVALID
+ * (use lx_sim_read_field).  The first call on a device looks up the array's device address
+ * and caches it, so make that first call before any stream capture begins.  All calls on a
+ * device share the array: calls whose GPU work overlaps (different streams or host threads
+ * at once) race, so order them. */
+LX_API lx_status lx_sim_read_field_noalloc(lx_sim* sim, int comp, double* host, size_t n);
 /* Number of completed steps. */
 LX_API int lx_sim_timestep(const lx_sim* sim);
 /* max over the grid of Ey^2 (planar) or Ex^2+Ey^2+Ez^2 (3D) after the last monitor step. */

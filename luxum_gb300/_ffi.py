@@ -88,6 +88,7 @@ def declare(lib) -> None:
     _proto(lib, "lx_sim_field_shape", C.c_int, sim, C.c_int, P(C.c_int))
     _proto(lib, "lx_sim_read_field", C.c_int, sim, C.c_int, P(C.c_double), C.c_size_t)
     _proto(lib, "lx_sim_write_field", C.c_int, sim, C.c_int, P(C.c_double), C.c_size_t)
+    _proto(lib, "lx_sim_read_field_noalloc", C.c_int, sim, C.c_int, P(C.c_double), C.c_size_t)
     _proto(lib, "lx_sim_timestep", C.c_int, sim)
     _proto(lib, "lx_sim_max_e2", C.c_int, sim, P(C.c_double))
     _proto(lib, "lx_sim_set_probes", C.c_int, sim, P(C.c_int), C.c_int, C.c_int)
