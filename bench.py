@@ -255,6 +255,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision", action="store_true", help="skip the FP32 / FP16-storage lines")
     ap.add_argument("--profile", type=int, default=0, metavar="N",
                     help="run the N^3 profiling case instead of the benchmark (for ncu)")
     ap.add_argument("--profile-steps", type=int, default=4)
@@ -388,11 +389,50 @@ def main():
         except (OSError, ValueError):
             pass
 
+    # ---- reduced-precision forms of the same workload: throughput and error vs this FP64 run
+    precision = {}
+    if not args.no_precision:
+        sim.reset()
+        sim.step(STEPS)
+        sim.sync()
+        ref = [sim.field(c) for c in range(6)]
+        for prec, name in ((1, "fp32"), (2, "fp16_storage")):
+            q = Sim(workload_params(prec))
+            q.set_stream(stream.cuda_stream)
+            for c in range(3):
+                q.set_material(c, F[c], 1e6)
+            q.set_probes(ijk, STEPS)
+            q.set_snapshots(SNAP_EVERY, 0x3F, sink)
+            q.reset()
+            q.step(STEPS)
+            q.sync()
+            barrier()
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for _ in range(args.steps):
+                q.reset()
+                q.step(STEPS)
+            q.sync()
+            f1.record(stream)
+            barrier()
+            qms = f0.elapsed_time(f1)
+            errs = {}
+            for grp, comps in (("E", (0, 1, 2)), ("H", (3, 4, 5))):
+                num = sum(float(np.linalg.norm(q.field(c) - ref[c])) ** 2 for c in comps)
+                den = sum(float(np.linalg.norm(ref[c])) ** 2 for c in comps)
+                errs[grp] = (num / den) ** 0.5 if den else None
+            kq = q.time_kernels(40)
+            precision[name] = {"value": cell_updates / (qms * 1e-3) / 1e9, "unit": UNIT,
+                               "ms_per_step": qms / args.steps, "speedup_vs_fp64": ms / qms,
+                               "rel_l2_vs_fp64_after_1000_steps": errs, "kernel_ms": kq}
+            q.close()
+        del ref
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_dict(),
             "e2e": e2e, "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches,
-            "max_e2_final": sim.max_e2()}
+            "max_e2_final": sim.max_e2(), "precision_forms": precision}
     sim.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

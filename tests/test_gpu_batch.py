@@ -1,0 +1,81 @@
+"""Batched stepping (lx_batch_*): every member must evolve exactly as it does alone.
+
+Members of mixed kinds (planar and 3-D, uniform and non-uniform spacing, with and without
+CPML, TF/SF and DFT planes) share launches; their fields, DFT accumulators and max|E|^2
+must equal those of twin handles stepped one by one, bit for bit, across graph replays,
+steps taken alone in between and removal of a member.
+"""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ["planar_pml_axis", "planar_oblique", "3d_pml_axis", "3d_pml_pulse_nonuniform"]
+
+
+def _make(name, precision):
+    from luxum_gb300 import Sim
+
+    p, steps, boxes = cases.build(name)
+    p.precision = precision
+    s = Sim(p)
+    for lo, hi, eps in boxes:
+        s.set_eps_box(lo, hi, eps)
+    if name in ("planar_pml_axis", "3d_pml_axis"):
+        w = 2 * np.pi * np.linspace(3e10, 1.5e11, 5)
+        s.add_dft_plane(0, 20, w, every=2 if name == "3d_pml_axis" else 1)
+    return s
+
+
+def _same(a, b):
+    for c in range(6):
+        if np.prod(a.shape(c)) == 0:
+            continue
+        assert np.array_equal(a.field(c), b.field(c)), c
+    for plane in getattr(a, "_dft", {}):
+        assert np.array_equal(a.dft(plane), b.dft(plane))
+    assert a.max_e2() == b.max_e2()
+    assert a.t == b.t
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_batch_equals_solo(engine, precision):
+    from luxum_gb300 import Batch
+
+    members = [_make(n, precision) for n in NAMES]
+    twins = [_make(n, precision) for n in NAMES]
+    batch = Batch(chunk=10)
+    for m in members:
+        batch.add(m)
+    assert len(batch) == 4
+    batch.step(37)  # 3 graph replays + 7 direct steps
+    for t in twins:
+        t.step(37)
+    for m, t in zip(members, twins):
+        _same(m, t)
+    members[2].step(5)  # a member steps alone between batch steps
+    twins[2].step(5)
+    batch.step(13)
+    for t in twins:
+        t.step(13)
+    for m, t in zip(members, twins):
+        _same(m, t)
+    batch.remove(members[1])
+    batch.step(20)
+    for i in (0, 2, 3):
+        twins[i].step(20)
+    for i in (0, 2, 3):
+        _same(members[i], twins[i])
+    batch.close()
+
+
+def test_batch_rejects_mixed_precision(engine):
+    from luxum_gb300 import Batch, LuxumError
+
+    a, b = _make("planar_oblique", 1), _make("planar_oblique", 0)
+    batch = Batch()
+    batch.add(a)
+    with pytest.raises(LuxumError):
+        batch.add(b)
