@@ -193,6 +193,223 @@ def run_cpu_sample(steps: int, threads: int):
     return N ** 3 * steps / dt / 1e9, dt
 
 
+def lens_sims(n_sims: int, seed: int, precision: int, steps: int):
+    """The batch workload: planar lens simulations of uneven size (seeded).
+
+    Side N ~ U{128..1024}; half elliptic lenses (semi-axes 10-40 % of N, eps_r ~ U(1.5, 2.25)),
+    half distorted lenses (same ellipse with a sinusoidal boundary perturbation of up to
+    5 cells); Ey plane wave at normal incidence from the left through a TF/SF box 16 cells
+    inside a 16-cell CPML (textbook CPML sign, kappa 5, a_max 0.05).  The lens enters as the
+    material array F of Cb = dt/(eps0*(1+F)), i.e. F = eps_r - 1.
+    """
+    from luxum_gb300 import Sim, params
+
+    rng = np.random.default_rng(seed)
+    sims = []
+    for q in range(n_sims):
+        n = int(rng.integers(128, 1025))
+        box = (32, n - 33)
+        p = params(isPlanar=1, Nx=n, Ny=1, Nz=n, dx=1e-3, dy=0.0, dz=1e-3, S=0.5, num_timesteps=steps, usePW=1,
+                   kx_pw=1.0, Ey_pw=1.0, off_pw=24.0, x1_pw=box[0], x2_pw=box[1], z1_pw=box[0], z2_pw=box[1],
+                   usePML=1, d_pml=0.016, sigma=0.65, sigma_m=3.0, kappa=5.0, a_max=0.05, a_m=1.0,
+                   cpml_mode=1, precision=precision)
+        s = Sim(p)
+        a, b = rng.uniform(0.1, 0.4, 2) * n
+        eps = rng.uniform(1.5, 2.25)
+        x = np.arange(n)[:, None] - n / 2
+        z = np.arange(n)[None, :] - n / 2
+        r2 = (x / a) ** 2 + (z / b) ** 2
+        if q % 2:
+            th = np.arctan2(z / b, x / a)
+            amp = rng.uniform(1.0, 5.0) / min(a, b)
+            m = int(rng.integers(3, 9))
+            inside = np.sqrt(r2) <= 1.0 + amp * np.sin(m * th + rng.uniform(0, 2 * np.pi))
+        else:
+            inside = r2 <= 1.0
+        F = np.where(inside, eps - 1.0, 0.0).reshape(n, 1, n)
+        s.set_material(1, F, 1.0)
+        sims.append(s)
+    return sims
+
+
+def bench_batch(args):
+    """--config batch: 256 uneven planar simulations stepped as one batch."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from luxum_gb300 import Batch
+
+    steps = args.batch_steps
+    sims = lens_sims(args.batch_sims, 4, 1, steps)
+    cells = sum(s.p.Nx * s.p.Nz for s in sims)
+    batch = Batch(chunk=100)
+    for s in sims:
+        batch.add(s)
+
+    def run():
+        for s in sims:
+            s.reset()
+        batch.step(steps)
+
+    run()  # warm-up: graph capture, first touch
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    value = cells * steps * args.steps / dt / 1e9
+    # the same simulations one by one (unbatched), on a sample
+    sample = sims[: args.solo_sample]
+    scells = sum(s.p.Nx * s.p.Nz for s in sample)
+    for s in sample:
+        s.reset()
+        s.step(100)
+        s.sync()
+    t0 = time.perf_counter()
+    for s in sample:
+        s.reset()
+        s.step(args.solo_steps)
+        s.sync()
+    solo = scells * args.solo_steps / (time.perf_counter() - t0) / 1e9
+    line = {"config": {"workload": f"batch of {len(sims)} planar lens simulations, sides U{{128..1024}} seed 4, "
+                                   f"CPML 16, TF/SF normal incidence, FP32, {steps} steps, graph chunks of 100",
+                       "cells": cells, "cell_updates_per_run": cells * steps},
+            "metric": "Gcell-updates/s (batched)", "value": value, "unit": UNIT, "runs": args.steps,
+            "s_per_run": dt / args.steps, "dtype": "f32",
+            "unbatched_sample": {"sims": len(sample), "value": solo, "steps": args.solo_steps,
+                                 "note": "same simulations stepped one handle at a time with lx_sim_step"},
+            "batched_over_unbatched": value / solo, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    batch.close()
+
+
+def serve_requests(n: int, seed: int, rate: float):
+    """Request stream: Poisson arrivals; 80 % planar (side log-uniform 256..2048), 20 % 3-D
+    (side log-uniform 64..256); 1-8 random dielectric boxes with eps_r ~ U(1, 12)."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    reqs = []
+    for q in range(n):
+        planar = rng.random() < 0.8
+        lo, hi = (256, 2048) if planar else (64, 256)
+        side = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+        m = serve_margin(side)
+        lo_b, hi_b = 2 * m + 2, side - 2 * m - 8  # scatterers between the TF/SF face and the monitor plane
+        boxes = []
+        for _ in range(int(rng.integers(1, 9))):
+            c0 = rng.integers(lo_b, hi_b, 3)
+            w = rng.integers(4, max(5, side // 6), 3)
+            a = np.maximum(c0 - w // 2, lo_b)
+            b = np.minimum(c0 + w // 2, hi_b)
+            boxes.append(((int(a[0]), 0 if planar else int(a[1]), int(a[2])),
+                          (int(b[0]), 1 if planar else int(b[1]), int(b[2])), float(rng.uniform(1.0, 12.0))))
+        reqs.append({"id": q, "arrival": float(t[q]), "planar": planar, "side": side, "boxes": boxes})
+    return reqs
+
+
+SERVE_STEPS = 2000
+
+
+def serve_margin(side: int) -> int:
+    """CPML depth (cells); the TF/SF box starts the same depth further in."""
+    return min(16, side // 8)
+SERVE_OMEGA = 2 * np.pi * np.linspace(0.5e9, 10e9, 64)  # monitor frequencies (rad/s)
+
+
+def serve_params(req):
+    from luxum_gb300 import params
+
+    n = req["side"]
+    m = serve_margin(n)
+    box = (2 * m, n - 1 - 2 * m)
+    kw = dict(dx=1e-3, dy=1e-3, dz=1e-3, S=0.5, num_timesteps=SERVE_STEPS, usePW=1, kx_pw=1.0, off_pw=56.0 - 2 * m,
+              x1_pw=box[0], x2_pw=box[1], y1_pw=box[0], y2_pw=box[1], z1_pw=box[0], z2_pw=box[1], usePML=1,
+              d_pml=m * 1e-3, sigma=0.65, sigma_m=3.0, kappa=5.0, a_max=0.05, a_m=1.0, cpml_mode=1, precision=1)
+    if req["planar"]:
+        return params(isPlanar=1, Nx=n, Ny=1, Nz=n, Ey_pw=1.0, y1_pw=0, y2_pw=0, **{k: v for k, v in kw.items()
+                                                                                 if k not in ("y1_pw", "y2_pw")})
+    return params(isPlanar=0, Nx=n, Ny=n, Nz=n, Ez_pw=1.0, **kw)
+
+
+def serve_sim(req):
+    """One request as a handle: dielectric boxes and a DFT plane 4 cells before the TF/SF box's far face."""
+    from luxum_gb300 import Sim
+
+    s = Sim(serve_params(req))
+    for lo, hi, eps in req["boxes"]:
+        s.set_eps_box(lo, hi, eps)
+    plane = s.add_dft_plane(0, req["side"] - 1 - 2 * serve_margin(req["side"]) - 4, SERVE_OMEGA, every=10)
+    return s, plane
+
+
+def bench_serve(args):
+    """--config serve: continuous batching of a Poisson request stream under an HBM budget."""
+    import collections
+
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from luxum_gb300 import Batch, device_bytes
+
+    reqs = serve_requests(args.serve_requests, 5, args.serve_rate)
+    budget = args.serve_budget_gb * 1e9
+    chunk = args.serve_chunk
+    for r in reqs:
+        r["bytes"] = device_bytes(serve_params(r)) + 4 * 64 * 16 * (r["side"] ** (1 if r["planar"] else 2))
+        r["cells"] = r["side"] ** (2 if r["planar"] else 3)
+    batch = Batch(chunk=chunk)
+    queue = collections.deque(reqs)
+    active = {}
+    used = 0.0
+    lat, peak_active, peak_bytes, work = [], 0, 0.0, 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with ClockSampler(0) as clk:
+        while queue or active:
+            now = time.perf_counter() - t0
+            while queue and queue[0]["arrival"] <= now and (used + queue[0]["bytes"] <= budget or not active):
+                r = queue.popleft()
+                s, plane = serve_sim(r)
+                batch.add(s)
+                active[id(s)] = (s, plane, r)
+                used += r["bytes"]
+            peak_active = max(peak_active, len(active))
+            peak_bytes = max(peak_bytes, used)
+            if not active:
+                time.sleep(max(0.0, queue[0]["arrival"] - (time.perf_counter() - t0)))
+                continue
+            batch.step(chunk)
+            for key in list(active):
+                s, plane, r = active[key]
+                if s.t >= SERVE_STEPS:
+                    flux = s.dft_flux(plane)
+                    assert np.all(np.isfinite(flux))
+                    lat.append(time.perf_counter() - t0 - r["arrival"])
+                    work += r["cells"] * SERVE_STEPS
+                    batch.remove(s)
+                    s.close()
+                    used -= r["bytes"]
+                    del active[key]
+        wall = time.perf_counter() - t0
+    lat = np.array(lat)
+    offered = sum(r["cells"] for r in reqs) * SERVE_STEPS / reqs[-1]["arrival"] / 1e9
+    line = {"config": {"workload": f"{len(reqs)} requests, Poisson {args.serve_rate}/s (seed 5), 80% planar 256-2048, "
+                                   f"20% 3-D 64-256, 1-8 eps boxes, {SERVE_STEPS} steps FP32, FP64 DFT 64 freqs at one "
+                                   f"plane (sampled every 10 steps), budget {args.serve_budget_gb} GB, chunk {chunk}"},
+            "metric": "p50/p99 latency and aggregate Gcell-updates/s", "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "value": work / wall / 1e9,
+            "unit": UNIT, "offered_gcells": offered, "wall_s": wall, "completed": int(lat.size),
+            "peak_active": peak_active, "peak_budget_gb": peak_bytes / 1e9, "dtype": "f32", "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    batch.close()
+
+
 def dist_setup(n_gpus: int):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -260,7 +477,21 @@ def main():
                     help="run the N^3 profiling case instead of the benchmark (for ncu)")
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--precision", type=int, default=0, help="profiling case precision: 0 fp64, 1 fp32, 2 fp16")
+    ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "serve"],
+                    help="drop-in: the headline 256^3 FP64 workload; batch: 256 uneven planar simulations")
+    ap.add_argument("--batch-sims", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=3000)
+    ap.add_argument("--solo-sample", type=int, default=16)
+    ap.add_argument("--solo-steps", type=int, default=300)
+    ap.add_argument("--serve-requests", type=int, default=1000)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-chunk", type=int, default=100)
     args = ap.parse_args()
+    if args.config == "batch":
+        return bench_batch(args)
+    if args.config == "serve":
+        return bench_serve(args)
     if args.profile:
         return profile_case(args.profile, args.profile_steps, args.precision)
     if args.warmup < 3:

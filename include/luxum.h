@@ -133,6 +133,11 @@ LX_API lx_status lx_params_from_yaml(const char* path, lx_params* p);
  * constants and CPML profiles exactly as maxwell.cc:60-148 / 997-1280. */
 LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out);
 LX_API void lx_sim_destroy(lx_sim* sim);
+/* Device memory lx_sim_create would hold for *p (fields, coefficients, CPML psi slabs and
+ * profiles, TF/SF tables), computed on the host without a GPU; snapshot staging, probes,
+ * DFT planes and transfer buffers come on top when used.  Serving loops admit requests
+ * against an HBM budget with it. */
+LX_API lx_status lx_params_device_bytes(const lx_params* p, size_t* bytes);
 /* Zeroes E, H, psi and |E|^2 and rewinds to step 0 (the state after lx_sim_create); keeps
  * Cb, probe positions and snapshot outputs, so one handle can run many simulations. */
 LX_API lx_status lx_sim_reset(lx_sim* sim);

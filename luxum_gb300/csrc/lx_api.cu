@@ -33,6 +33,27 @@ lx_status set_thread_error(const char* msg, lx_status st) {
 }
 }  // namespace lx
 
+// Device memory of handles and batches comes from the device's stream-ordered pool: creating
+// and destroying handles (the serving loop does so continuously) then neither pays for a
+// fresh cudaMalloc nor synchronises the device as cudaFree does.  Freed blocks stay in the
+// pool for reuse (release threshold raised once per process); cudaMemPoolTrimTo on the
+// device's default pool returns them.
+static void keep_pool_memory() {
+  static bool done = false;
+  if (done) return;
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done = true;
+}
+
+static void dfree(void* p, cudaStream_t st) {
+  if (p) cudaFreeAsync(p, st);
+}
+
 static lx_status fail(lx_sim* s, lx_status st, const std::string& msg) {
   if (s) s->err = msg;
   g_err = msg;
@@ -303,8 +324,8 @@ template <class C>
 static lx_status upload_vec(lx_sim* s, void** dst, const std::vector<double>& v) {
   std::vector<C> tmp(v.size());
   for (size_t q = 0; q < v.size(); q++) tmp[q] = (C)v[q];
-  CK(cudaMalloc(dst, tmp.size() * sizeof(C) + 16));
-  CK(cudaMemcpy(*dst, tmp.data(), tmp.size() * sizeof(C), cudaMemcpyHostToDevice));
+  CK(cudaMallocAsync(dst, tmp.size() * sizeof(C) + 16, s->own));
+  CK(cudaMemcpyAsync(*dst, tmp.data(), tmp.size() * sizeof(C), cudaMemcpyHostToDevice, s->own));
   s->n_h2d += tmp.size() * sizeof(C);
   return LX_OK;
 }
@@ -335,24 +356,29 @@ extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
   if (!s) return;
   stop_writer(s);
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->side) cudaStreamSynchronize(s->side);
+  cudaStream_t fs = s->own;
   for (int c = 0; c < 3; c++) {
-    cudaFree(s->E[c]); cudaFree(s->H[c]); cudaFree(s->Cbs[c]);
-    for (int q = 0; q < 6; q++) cudaFree(s->prof[c][q]);
-    for (int q = 0; q < 2; q++) { cudaFree(s->psiH[c][q]); cudaFree(s->psiE[c][q]); }
+    dfree(s->E[c], fs); dfree(s->H[c], fs); dfree(s->Cbs[c], fs);
+    for (int q = 0; q < 6; q++) dfree(s->prof[c][q], fs);
+    for (int q = 0; q < 2; q++) { dfree(s->psiH[c][q], fs); dfree(s->psiE[c][q], fs); }
   }
-  cudaFree(s->tab); cudaFree(s->d_max); cudaFree(s->etotal); cudaFree(s->xfer);
-  cudaFree(s->d_probe_ijk); cudaFree(s->d_probe);
+  dfree(s->tab, fs); dfree(s->d_max, fs); dfree(s->etotal, fs); dfree(s->xfer, fs);
+  dfree(s->d_probe_ijk, fs); dfree(s->d_probe, fs);
   for (auto& sl : s->slots) {
-    cudaFree(sl.dev);
+    dfree(sl.dev, fs);
     if (sl.host) cudaFreeHost(sl.host);
     if (sl.ev_d2h) cudaEventDestroy(sl.ev_d2h);
   }
   for (auto& o : s->outputs) delete o.h5;
   for (auto& d : s->dfts) {
-    cudaFree(d.d_omega);
-    cudaFree(d.d_acc);
+    dfree(d.d_omega, fs);
+    dfree(d.d_acc, fs);
   }
-  if (s->own) cudaStreamDestroy(s->own);
+  if (s->own) {
+    cudaStreamSynchronize(s->own);
+    cudaStreamDestroy(s->own);
+  }
   if (s->side) cudaStreamDestroy(s->side);
   delete s;
 }
@@ -360,8 +386,8 @@ extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
 static lx_status alloc_zero(lx_sim* s, void** p, size_t bytes) {
   *p = nullptr;
   if (bytes == 0) return LX_OK;
-  CK(cudaMalloc(p, bytes));
-  CK(cudaMemsetAsync(*p, 0, bytes, s->stream));
+  CK(cudaMallocAsync(p, bytes, s->own));
+  CK(cudaMemsetAsync(*p, 0, bytes, s->own));
   return LX_OK;
 }
 
@@ -435,21 +461,16 @@ static lx_status create_typed(lx_sim* s) {
   }
   if (s->tfsf) {
     build_sets(s);
-    CK(cudaMalloc(&s->tab, (size_t)(s->tab_total > 0 ? s->tab_total : 1) * sizeof(C)));
+    CK(cudaMallocAsync(&s->tab, (size_t)(s->tab_total > 0 ? s->tab_total : 1) * sizeof(C), s->own));
   }
-  CK(cudaMalloc(&s->d_max, 64));
-  CK(cudaMemsetAsync(s->d_max, 0, 64, s->stream));
+  CK(cudaMallocAsync(&s->d_max, 64, s->own));
+  CK(cudaMemsetAsync(s->d_max, 0, 64, s->own));
   return LX_OK;
 }
 
-extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
-  if (!p || !out) return fail(nullptr, LX_ERR_INVALID, "null argument");
-  *out = nullptr;
-  std::string why;
-  lx_status st = validate(p, why);
-  if (st) return fail(nullptr, st, why);
-  lx_sim* s = new (std::nothrow) lx_sim();
-  if (!s) return fail(nullptr, LX_ERR_OOM, "host allocation failed");
+// Host-side set-up shared by lx_sim_create and lx_params_device_bytes: grid, constants
+// (maxwell.cc:60-148), plane-wave clipping, point source.
+static void setup_host(lx_sim* s, const lx_params* p) {
   s->p = *p;
   s->planar = p->isPlanar != 0;
   s->pml = p->usePML != 0;
@@ -516,6 +537,19 @@ extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
     }
   }
 
+}
+
+extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
+  if (!p || !out) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  *out = nullptr;
+  std::string why;
+  lx_status st = validate(p, why);
+  if (st) return fail(nullptr, st, why);
+  lx_sim* s = new (std::nothrow) lx_sim();
+  if (!s) return fail(nullptr, LX_ERR_OOM, "host allocation failed");
+  keep_pool_memory();
+  setup_host(s, p);
+
   cudaError_t e = cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -535,6 +569,39 @@ extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
     return fail(nullptr, st, m);
   }
   *out = s;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_params_device_bytes(const lx_params* p, size_t* bytes) {
+  if (!p || !bytes) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  std::string why;
+  lx_status st = validate(p, why);
+  if (st) return fail(nullptr, st, why);
+  lx_sim tmp;
+  setup_host(&tmp, p);
+  size_t b = 0;
+  const int nE = tmp.planar ? 1 : 3, nH = tmp.planar ? 2 : 3;
+  b += (size_t)(nE + nH) * tmp.ncell * tmp.tsize + (size_t)nE * tmp.ncell * tmp.csize;
+  if (tmp.pml) {
+    for (int a = 0; a < 3; a++) {
+      if (tmp.planar && a == 1) continue;
+      const int N = a == 0 ? p->Nx : (a == 1 ? p->Ny : p->Nz);
+      const double delta = a == 0 ? p->dx : (a == 1 ? p->dy : p->dz);
+      AxisProf ap;
+      axis_profiles(tmp.k, p->cpml_mode, N, delta, ap);
+      tmp.slab[a] = make_slab(ap, N);
+      b += (size_t)(6 * N) * tmp.csize + 96;
+      const Slab& sl = tmp.slab[a];
+      const size_t plane = a == 0 ? (size_t)tmp.Ny * tmp.Nzp : (a == 1 ? (size_t)tmp.Nx * tmp.Nzp : (size_t)tmp.Nx * tmp.Ny);
+      // psi arrays whose derivative runs along this axis: 4 in 3-D (2 H + 2 E), 2 in planar
+      b += (size_t)(tmp.planar ? 2 : 4) * sl.n * plane * tmp.csize;
+    }
+  }
+  if (tmp.tfsf) {
+    build_sets(&tmp);
+    b += (size_t)tmp.tab_total * tmp.csize;
+  }
+  *bytes = b + 64;
   return LX_OK;
 }
 
@@ -565,7 +632,8 @@ static lx_status ensure_xfer(lx_sim* s) {
   if (s->xfer) return LX_OK;
   size_t m = 0;
   for (int c = 0; c < 7; c++) m = std::max(m, ext_n(s, c));
-  CK(cudaMalloc(&s->xfer, m * sizeof(double) + 64));
+  CK(cudaMallocAsync(&s->xfer, m * sizeof(double) + 64, s->own));
+  CK(cudaStreamSynchronize(s->own));
   s->xfer_cap = m;
   return LX_OK;
 }
@@ -696,18 +764,19 @@ extern "C" LX_API lx_status lx_sim_set_probes(lx_sim* s, const int* ijk, int npr
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
   if (nprobes < 0 || nprobes > lx::kMaxProbes || cap < 0) return fail(s, LX_ERR_INVALID, "0..64 probes, capacity >= 0");
   CK(cudaStreamSynchronize(s->stream));
-  cudaFree(s->d_probe_ijk);
-  cudaFree(s->d_probe);
+  dfree(s->d_probe_ijk, s->own);
+  dfree(s->d_probe, s->own);
   s->d_probe_ijk = nullptr;
   s->d_probe = nullptr;
   s->nprobes = 0;
   s->probe_cap = 0;
   s->probe_rows = 0;
   if (nprobes == 0 || cap == 0) return LX_OK;
-  CK(cudaMalloc(&s->d_probe_ijk, sizeof(int) * 3 * nprobes));
-  CK(cudaMemcpy(s->d_probe_ijk, ijk, sizeof(int) * 3 * nprobes, cudaMemcpyHostToDevice));
-  CK(cudaMalloc(&s->d_probe, sizeof(double) * 6 * (size_t)nprobes * cap));
-  CK(cudaMemset(s->d_probe, 0, sizeof(double) * 6 * (size_t)nprobes * cap));
+  CK(cudaMallocAsync(&s->d_probe_ijk, sizeof(int) * 3 * nprobes, s->own));
+  CK(cudaMemcpyAsync(s->d_probe_ijk, ijk, sizeof(int) * 3 * nprobes, cudaMemcpyHostToDevice, s->own));
+  CK(cudaMallocAsync(&s->d_probe, sizeof(double) * 6 * (size_t)nprobes * cap, s->own));
+  CK(cudaMemsetAsync(s->d_probe, 0, sizeof(double) * 6 * (size_t)nprobes * cap, s->own));
+  CK(cudaStreamSynchronize(s->own));
   s->nprobes = nprobes;
   s->probe_cap = cap;
   return LX_OK;
@@ -745,10 +814,12 @@ extern "C" LX_API lx_status lx_sim_add_dft_plane(lx_sim* s, int axis, int index,
   for (int q = 0; q < 4; q++) d.comps[q] = kComps[axis][q];
   d.omega.assign(omega, omega + nfreq);
   d.n_acc = (size_t)nfreq * 4 * d.na * d.nb * 2;
-  CK(cudaMalloc(&d.d_omega, nfreq * sizeof(double)));
-  CK(cudaMemcpy(d.d_omega, omega, nfreq * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMalloc(&d.d_acc, d.n_acc * sizeof(double)));
-  CK(cudaMemset(d.d_acc, 0, d.n_acc * sizeof(double)));
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMallocAsync(&d.d_omega, nfreq * sizeof(double), s->own));
+  CK(cudaMemcpyAsync(d.d_omega, omega, nfreq * sizeof(double), cudaMemcpyHostToDevice, s->own));
+  CK(cudaMallocAsync(&d.d_acc, d.n_acc * sizeof(double), s->own));
+  CK(cudaMemsetAsync(d.d_acc, 0, d.n_acc * sizeof(double), s->own));
+  CK(cudaStreamSynchronize(s->own));
   s->n_h2d += nfreq * sizeof(double);
   s->dfts.push_back(d);
   *id = (int)s->dfts.size() - 1;
@@ -857,20 +928,21 @@ static lx_status add_output(lx_sim* s, const lx::Output& o) {
     if (all & (1u << c)) need += ext_n(s, c);
   for (auto& sl : s->slots) {
     if (sl.cap >= need) continue;
-    cudaFree(sl.dev);
+    dfree(sl.dev, s->own);
     if (sl.host) cudaFreeHost(sl.host);
     sl.dev = nullptr;
     sl.host = nullptr;
-    CK(cudaMalloc(&sl.dev, need * sizeof(double)));
+    CK(cudaMallocAsync(&sl.dev, need * sizeof(double), s->own));
     CK(cudaHostAlloc(&sl.host, need * sizeof(double), cudaHostAllocDefault));
     if (!sl.ev_d2h) CK(cudaEventCreateWithFlags(&sl.ev_d2h, cudaEventDisableTiming));
     sl.cap = need;
   }
   if ((all & (1u << LX_ETOTAL)) && !s->etotal) {
     if (s->planar) return fail(s, LX_ERR_INVALID, "|E|^2 snapshots exist for 3-D grids only");
-    CK(cudaMalloc(&s->etotal, s->ncell * s->csize));
-    CK(cudaMemset(s->etotal, 0, s->ncell * s->csize));
+    CK(cudaMallocAsync(&s->etotal, s->ncell * s->csize, s->own));
+    CK(cudaMemsetAsync(s->etotal, 0, s->ncell * s->csize, s->own));
   }
+  CK(cudaStreamSynchronize(s->own));
   if (!s->writer_on) {
     s->writer = std::thread(writer_main, s);
     s->writer_on = true;
@@ -1276,14 +1348,14 @@ struct lx_batch {
 
 static void batch_free_device(lx_batch* b) {
   for (auto& g : b->groups) {
-    cudaFree(g.d_params);
-    cudaFree(g.d_tiles);
+    dfree(g.d_params, b->stream);
+    dfree(g.d_tiles, b->stream);
   }
   b->groups.clear();
-  cudaFree(b->d_pps);
-  cudaFree(b->d_ts);
-  cudaFree(b->d_slots);
-  cudaFree(b->d_dfts);
+  dfree(b->d_pps, b->stream);
+  dfree(b->d_ts, b->stream);
+  dfree(b->d_slots, b->stream);
+  dfree(b->d_dfts, b->stream);
   b->d_pps = nullptr;
   b->d_ts = nullptr;
   b->d_slots = nullptr;
@@ -1376,7 +1448,7 @@ static lx_status batch_rebuild(lx_batch* b) {
   b->need_prologue = false;
   b->max_cells4 = 0;
   b->host_ts.resize(n);
-  BCK(cudaMalloc(&b->d_slots, sizeof(unsigned long long) * (n > 0 ? n : 1)));
+  BCK(cudaMallocAsync(&b->d_slots, sizeof(unsigned long long) * (n > 0 ? n : 1), b->stream));
   for (int q = 0; q < n; q++) {
     lx_sim* s = b->sims[q];
     pps[q] = make_prologue(s);
@@ -1410,14 +1482,14 @@ static lx_status batch_rebuild(lx_batch* b) {
     b->groups[gi].members.push_back(q);
   }
   b->need_prologue = n > 0;  // monitor slots are reset every step
-  BCK(cudaMalloc(&b->d_pps, sizeof(lx::PrologueParams) * (n > 0 ? n : 1)));
-  BCK(cudaMemcpy(b->d_pps, pps.data(), sizeof(lx::PrologueParams) * n, cudaMemcpyHostToDevice));
-  BCK(cudaMalloc(&b->d_ts, sizeof(int) * (n > 0 ? n : 1)));
-  BCK(cudaMemcpy(b->d_ts, b->host_ts.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  BCK(cudaMallocAsync(&b->d_pps, sizeof(lx::PrologueParams) * (n > 0 ? n : 1), b->stream));
+  BCK(cudaMemcpyAsync(b->d_pps, pps.data(), sizeof(lx::PrologueParams) * n, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMallocAsync(&b->d_ts, sizeof(int) * (n > 0 ? n : 1), b->stream));
+  BCK(cudaMemcpyAsync(b->d_ts, b->host_ts.data(), sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
   b->ndft = (int)dfts.size();
   if (b->ndft) {
-    BCK(cudaMalloc(&b->d_dfts, sizeof(lx::DftParams) * b->ndft));
-    BCK(cudaMemcpy(b->d_dfts, dfts.data(), sizeof(lx::DftParams) * b->ndft, cudaMemcpyHostToDevice));
+    BCK(cudaMallocAsync(&b->d_dfts, sizeof(lx::DftParams) * b->ndft, b->stream));
+    BCK(cudaMemcpyAsync(b->d_dfts, dfts.data(), sizeof(lx::DftParams) * b->ndft, cudaMemcpyHostToDevice, b->stream));
   }
   for (auto& g : b->groups) {
     std::vector<lx::StepParams<T, C>> ps;
@@ -1439,10 +1511,10 @@ static lx_status batch_rebuild(lx_batch* b) {
     }
     if ((long long)tiles.size() > 0x7fffffffLL) return bfail(b, LX_ERR_INVALID, "batch too large for one launch");
     g.ntiles = (int)tiles.size();
-    BCK(cudaMalloc(&g.d_params, sizeof(lx::StepParams<T, C>) * ps.size()));
-    BCK(cudaMemcpy(g.d_params, ps.data(), sizeof(lx::StepParams<T, C>) * ps.size(), cudaMemcpyHostToDevice));
-    BCK(cudaMalloc(&g.d_tiles, sizeof(lx::Tile) * (tiles.empty() ? 1 : tiles.size())));
-    BCK(cudaMemcpy(g.d_tiles, tiles.data(), sizeof(lx::Tile) * tiles.size(), cudaMemcpyHostToDevice));
+    BCK(cudaMallocAsync(&g.d_params, sizeof(lx::StepParams<T, C>) * ps.size(), b->stream));
+    BCK(cudaMemcpyAsync(g.d_params, ps.data(), sizeof(lx::StepParams<T, C>) * ps.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMallocAsync(&g.d_tiles, sizeof(lx::Tile) * (tiles.empty() ? 1 : tiles.size()), b->stream));
+    BCK(cudaMemcpyAsync(g.d_tiles, tiles.data(), sizeof(lx::Tile) * tiles.size(), cudaMemcpyHostToDevice, b->stream));
   }
   b->dirty = false;
   return LX_OK;

@@ -209,17 +209,25 @@ __device__ __forceinline__ unsigned long long e2_bits(float v) {
 template <class T, class C, bool UNI>
 __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k) {
   const long long c = (long long)i * p.si + (long long)j * p.sj + k;
+  const bool ux = (j < p.Ny - 1 && k < p.Nz - 1), uy = (i < p.Nx - 1 && k < p.Nz - 1), uz = (i < p.Nx - 1 && j < p.Ny - 1);
+  // Every load is issued before any store: the field arrays may alias as far as the compiler
+  // knows, so interleaving would serialise one memory round trip per component.
   const C ex = ld<T, C>(p.E[0] + c), ey = ld<T, C>(p.E[1] + c), ez = ld<T, C>(p.E[2] + c);
+  const C ez_j = ux ? ld<T, C>(p.E[2] + c + p.sj) : C(0), ey_k = ux ? ld<T, C>(p.E[1] + c + 1) : C(0);
+  const C ex_k = uy ? ld<T, C>(p.E[0] + c + 1) : C(0), ez_i = uy ? ld<T, C>(p.E[2] + c + p.si) : C(0);
+  const C ey_i = uz ? ld<T, C>(p.E[1] + c + p.si) : C(0), ex_j = uz ? ld<T, C>(p.E[0] + c + p.sj) : C(0);
+  const C hx = ux ? ld<T, C>(p.H[0] + c) : C(0), hy = uy ? ld<T, C>(p.H[1] + c) : C(0),
+          hz = uz ? ld<T, C>(p.H[2] + c) : C(0);
   int sx = -1, sy = -1, sz = -1;
   if (p.pml) {
     sx = slab_index(p.slab[0], i);
     sy = slab_index(p.slab[1], j);
     sz = slab_index(p.slab[2], k);
   }
+  C nhx = hx, nhy = hy, nhz = hz;
   // Hx: i < Nx, j < Ny-1, k < Nz-1; part 1 = dEz/dy (y profile), part 2 = dEy/dz (z profile)
-  if (j < p.Ny - 1 && k < p.Nz - 1) {
-    C d1 = ld<T, C>(p.E[2] + c + p.sj) - ez;
-    C d2 = ld<T, C>(p.E[1] + c + 1) - ey;
+  if (ux) {
+    C d1 = ez_j - ez, d2 = ey_k - ey;
     if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
     if (p.tfsf) {
       tfsf_apply<C>(p.setsH[0][0], p.tab, i, j, k, d1);
@@ -227,13 +235,11 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
     }
     if (sy >= 0) d1 = pml_term<C>(d1, p.psiH[0][0] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bH[1][j], p.cH[1][j], p.rkH[1][j]);
     if (sz >= 0) d2 = pml_term<C>(d2, p.psiH[0][1] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bH[2][k], p.cH[2][k], p.rkH[2][k]);
-    const C h = ld<T, C>(p.H[0] + c);
-    st<T, C>(p.H[0] + c, fmaC(-p.Dbs, d1 - d2, h));
+    nhx = fmaC(-p.Dbs, d1 - d2, hx);
   }
   // Hy: i < Nx-1, j < Ny, k < Nz-1; part 1 = dEx/dz (z), part 2 = dEz/dx (x)
-  if (i < p.Nx - 1 && k < p.Nz - 1) {
-    C d1 = ld<T, C>(p.E[0] + c + 1) - ex;
-    C d2 = ld<T, C>(p.E[2] + c + p.si) - ez;
+  if (uy) {
+    C d1 = ex_k - ex, d2 = ez_i - ez;
     if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
     if (p.tfsf) {
       tfsf_apply<C>(p.setsH[1][0], p.tab, i, j, k, d1);
@@ -241,13 +247,11 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
     }
     if (sz >= 0) d1 = pml_term<C>(d1, p.psiH[1][0] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bH[2][k], p.cH[2][k], p.rkH[2][k]);
     if (sx >= 0) d2 = pml_term<C>(d2, p.psiH[1][1] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bH[0][i], p.cH[0][i], p.rkH[0][i]);
-    const C h = ld<T, C>(p.H[1] + c);
-    st<T, C>(p.H[1] + c, fmaC(-p.Dbs, d1 - d2, h));
+    nhy = fmaC(-p.Dbs, d1 - d2, hy);
   }
   // Hz: i < Nx-1, j < Ny-1, k < Nz; part 1 = dEy/dx (x), part 2 = dEx/dy (y)
-  if (i < p.Nx - 1 && j < p.Ny - 1) {
-    C d1 = ld<T, C>(p.E[1] + c + p.si) - ey;
-    C d2 = ld<T, C>(p.E[0] + c + p.sj) - ex;
+  if (uz) {
+    C d1 = ey_i - ey, d2 = ex_j - ex;
     if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
     if (p.tfsf) {
       tfsf_apply<C>(p.setsH[2][0], p.tab, i, j, k, d1);
@@ -255,9 +259,11 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
     }
     if (sx >= 0) d1 = pml_term<C>(d1, p.psiH[2][0] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bH[0][i], p.cH[0][i], p.rkH[0][i]);
     if (sy >= 0) d2 = pml_term<C>(d2, p.psiH[2][1] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bH[1][j], p.cH[1][j], p.rkH[1][j]);
-    const C h = ld<T, C>(p.H[2] + c);
-    st<T, C>(p.H[2] + c, fmaC(-p.Dbs, d1 - d2, h));
+    nhz = fmaC(-p.Dbs, d1 - d2, hz);
   }
+  if (ux) st<T, C>(p.H[0] + c, nhx);
+  if (uy) st<T, C>(p.H[1] + c, nhy);
+  if (uz) st<T, C>(p.H[2] + c, nhz);
 }
 
 template <class T, class C, bool UNI>
@@ -274,73 +280,70 @@ __global__ void __launch_bounds__(256) h_kernel_3d(const StepParams<T, C> p) {
 // Returns the bit pattern of this cell's |E|^2 when monitoring (0 otherwise).
 template <class T, class C, bool UNI>
 __device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k) {
+  const long long c = (long long)i * p.si + (long long)j * p.sj + k;
+  const bool ii = (i >= 1 && i < p.Nx - 1), jj = (j >= 1 && j < p.Ny - 1), kk = (k >= 1 && k < p.Nz - 1);
+  const bool ux = (i < p.Nx - 1 && jj && kk), uy = (ii && j < p.Ny - 1 && kk), uz = (ii && jj && k < p.Nz - 1);
+  const bool mon = (p.max_slot != nullptr || p.etotal != nullptr) && i < p.Nx - 1 && j < p.Ny - 1 && k < p.Nz - 1;
+  // all loads first (see h_cell_3d)
+  const C hx = ld<T, C>(p.H[0] + c), hy = ld<T, C>(p.H[1] + c), hz = ld<T, C>(p.H[2] + c);
+  const C hz_j = ux ? ld<T, C>(p.H[2] + c - p.sj) : C(0), hy_k = ux ? ld<T, C>(p.H[1] + c - 1) : C(0);
+  const C hx_k = uy ? ld<T, C>(p.H[0] + c - 1) : C(0), hz_i = uy ? ld<T, C>(p.H[2] + c - p.si) : C(0);
+  const C hy_i = uz ? ld<T, C>(p.H[1] + c - p.si) : C(0), hx_j = uz ? ld<T, C>(p.H[0] + c - p.sj) : C(0);
+  const C ex = (ux || mon) ? ld<T, C>(p.E[0] + c) : C(0), ey = (uy || mon) ? ld<T, C>(p.E[1] + c) : C(0),
+          ez = (uz || mon) ? ld<T, C>(p.E[2] + c) : C(0);
+  const C cbx = ux ? p.Cbs[0][c] : C(0), cby = uy ? p.Cbs[1][c] : C(0), cbz = uz ? p.Cbs[2][c] : C(0);
+  int sx = -1, sy = -1, sz = -1;
+  if (p.pml) {
+    sx = slab_index(p.slab[0], i);
+    sy = slab_index(p.slab[1], j);
+    sz = slab_index(p.slab[2], k);
+  }
+  C exn = ex, eyn = ey, ezn = ez;
+  // Ex: i < Nx-1, j in [1,Ny-2], k in [1,Nz-2]; part 1 = dHz/dy (y), part 2 = dHy/dz (z)
+  if (ux) {
+    C d1 = hz - hz_j, d2 = hy - hy_k;
+    if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
+    if (p.tfsf) {
+      tfsf_apply<C>(p.setsE[0][0], p.tab, i, j, k, d1);
+      tfsf_apply<C>(p.setsE[0][1], p.tab, i, j, k, d2);
+    }
+    if (sy >= 0) d1 = pml_term<C>(d1, p.psiE[0][0] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bE[1][j], p.cE[1][j], p.rkE[1][j]);
+    if (sz >= 0) d2 = pml_term<C>(d2, p.psiE[0][1] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
+    exn = fmaC(cbx, d1 - d2, ex);
+  }
+  // Ey: i in [1,Nx-2], j < Ny-1, k in [1,Nz-2]; part 1 = dHx/dz (z), part 2 = dHz/dx (x)
+  if (uy) {
+    C d1 = hx - hx_k, d2 = hz - hz_i;
+    if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
+    if (p.tfsf) {
+      tfsf_apply<C>(p.setsE[1][0], p.tab, i, j, k, d1);
+      tfsf_apply<C>(p.setsE[1][1], p.tab, i, j, k, d2);
+    }
+    if (sz >= 0) d1 = pml_term<C>(d1, p.psiE[1][0] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
+    if (sx >= 0) d2 = pml_term<C>(d2, p.psiE[1][1] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
+    eyn = fmaC(cby, d1 - d2, ey);
+  }
+  // Ez: i in [1,Nx-2], j in [1,Ny-2], k < Nz-1; part 1 = dHy/dx (x), part 2 = dHx/dy (y)
+  if (uz) {
+    C d1 = hy - hy_i, d2 = hx - hx_j;
+    if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
+    if (p.tfsf) {
+      tfsf_apply<C>(p.setsE[2][0], p.tab, i, j, k, d1);
+      tfsf_apply<C>(p.setsE[2][1], p.tab, i, j, k, d2);
+    }
+    if (sx >= 0) d1 = pml_term<C>(d1, p.psiE[2][0] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
+    if (sy >= 0) d2 = pml_term<C>(d2, p.psiE[2][1] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bE[1][j], p.cE[1][j], p.rkE[1][j]);
+    ezn = fmaC(cbz, d1 - d2, ez);
+  }
+  if (ux) st<T, C>(p.E[0] + c, exn);
+  if (uy) st<T, C>(p.E[1] + c, eyn);
+  if (uz) st<T, C>(p.E[2] + c, ezn);
   unsigned long long mbits = 0ull;
-  {
-    const long long c = (long long)i * p.si + (long long)j * p.sj + k;
-    const C hx = ld<T, C>(p.H[0] + c), hy = ld<T, C>(p.H[1] + c), hz = ld<T, C>(p.H[2] + c);
-    int sx = -1, sy = -1, sz = -1;
-    if (p.pml) {
-      sx = slab_index(p.slab[0], i);
-      sy = slab_index(p.slab[1], j);
-      sz = slab_index(p.slab[2], k);
-    }
-    const bool ii = (i >= 1 && i < p.Nx - 1), jj = (j >= 1 && j < p.Ny - 1), kk = (k >= 1 && k < p.Nz - 1);
-    const bool mon = (p.max_slot != nullptr || p.etotal != nullptr) && i < p.Nx - 1 && j < p.Ny - 1 && k < p.Nz - 1;
-    C exn = 0, eyn = 0, ezn = 0;
-    // Ex: i < Nx-1, j in [1,Ny-2], k in [1,Nz-2]; part 1 = dHz/dy (y), part 2 = dHy/dz (z)
-    if (i < p.Nx - 1 && jj && kk) {
-      C d1 = hz - ld<T, C>(p.H[2] + c - p.sj);
-      C d2 = hy - ld<T, C>(p.H[1] + c - 1);
-      if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
-      if (p.tfsf) {
-        tfsf_apply<C>(p.setsE[0][0], p.tab, i, j, k, d1);
-        tfsf_apply<C>(p.setsE[0][1], p.tab, i, j, k, d2);
-      }
-      if (sy >= 0) d1 = pml_term<C>(d1, p.psiE[0][0] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bE[1][j], p.cE[1][j], p.rkE[1][j]);
-      if (sz >= 0) d2 = pml_term<C>(d2, p.psiE[0][1] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
-      exn = fmaC(p.Cbs[0][c], d1 - d2, ld<T, C>(p.E[0] + c));
-      st<T, C>(p.E[0] + c, exn);
-    } else if (mon) {
-      exn = ld<T, C>(p.E[0] + c);
-    }
-    // Ey: i in [1,Nx-2], j < Ny-1, k in [1,Nz-2]; part 1 = dHx/dz (z), part 2 = dHz/dx (x)
-    if (ii && j < p.Ny - 1 && kk) {
-      C d1 = hx - ld<T, C>(p.H[0] + c - 1);
-      C d2 = hz - ld<T, C>(p.H[2] + c - p.si);
-      if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
-      if (p.tfsf) {
-        tfsf_apply<C>(p.setsE[1][0], p.tab, i, j, k, d1);
-        tfsf_apply<C>(p.setsE[1][1], p.tab, i, j, k, d2);
-      }
-      if (sz >= 0) d1 = pml_term<C>(d1, p.psiE[1][0] + psi_index(2, p.slab[2], sz, i, j, k, p.Ny, p.Nzp), p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
-      if (sx >= 0) d2 = pml_term<C>(d2, p.psiE[1][1] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
-      eyn = fmaC(p.Cbs[1][c], d1 - d2, ld<T, C>(p.E[1] + c));
-      st<T, C>(p.E[1] + c, eyn);
-    } else if (mon) {
-      eyn = ld<T, C>(p.E[1] + c);
-    }
-    // Ez: i in [1,Nx-2], j in [1,Ny-2], k < Nz-1; part 1 = dHy/dx (x), part 2 = dHx/dy (y)
-    if (ii && jj && k < p.Nz - 1) {
-      C d1 = hy - ld<T, C>(p.H[1] + c - p.si);
-      C d2 = hx - ld<T, C>(p.H[0] + c - p.sj);
-      if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
-      if (p.tfsf) {
-        tfsf_apply<C>(p.setsE[2][0], p.tab, i, j, k, d1);
-        tfsf_apply<C>(p.setsE[2][1], p.tab, i, j, k, d2);
-      }
-      if (sx >= 0) d1 = pml_term<C>(d1, p.psiE[2][0] + psi_index(0, p.slab[0], sx, i, j, k, p.Ny, p.Nzp), p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
-      if (sy >= 0) d2 = pml_term<C>(d2, p.psiE[2][1] + psi_index(1, p.slab[1], sy, i, j, k, p.Ny, p.Nzp), p.bE[1][j], p.cE[1][j], p.rkE[1][j]);
-      ezn = fmaC(p.Cbs[2][c], d1 - d2, ld<T, C>(p.E[2] + c));
-      st<T, C>(p.E[2] + c, ezn);
-    } else if (mon) {
-      ezn = ld<T, C>(p.E[2] + c);
-    }
-    if (mon) {
-      // Etotal = Ez*Ez + Ey*Ey + Ex*Ex (three_dim_pml.cc:270), same association order
-      C e2 = fmaC(exn, exn, fmaC(eyn, eyn, ezn * ezn));
-      if (p.etotal) p.etotal[c] = e2;
-      mbits = e2_bits(e2);
-    }
+  if (mon) {
+    // Etotal = Ez*Ez + Ey*Ey + Ex*Ex (three_dim_pml.cc:270), same association order
+    const C e2 = fmaC(exn, exn, fmaC(eyn, eyn, ezn * ezn));
+    if (p.etotal) p.etotal[c] = e2;
+    mbits = e2_bits(e2);
   }
   return mbits;
 }
@@ -360,29 +363,35 @@ __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
 template <class T, class C, bool UNI>
 __device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i, const int k) {
   const long long c = (long long)i * p.si + k;
+  const bool ux = k < p.Nz - 1, uz = i < p.Nx - 1;
   const C ey = ld<T, C>(p.E[1] + c);
+  const C ey_k = ux ? ld<T, C>(p.E[1] + c + 1) : C(0), ey_i = uz ? ld<T, C>(p.E[1] + c + p.si) : C(0);
+  const C hx = ux ? ld<T, C>(p.H[0] + c) : C(0), hz = uz ? ld<T, C>(p.H[2] + c) : C(0);
+  C nhx = hx, nhz = hz;
   // Hx: k < Nz-1; Hx -= Db*(-curl2/kappa - psi2), curl2 = dEy/dz (z profile)
-  if (k < p.Nz - 1) {
-    C d2 = ld<T, C>(p.E[1] + c + 1) - ey;
+  if (ux) {
+    C d2 = ey_k - ey;
     if (!UNI) d2 *= p.rd[2];
     if (p.tfsf) tfsf_apply<C>(p.setsH[0][1], p.tab, i, 0, k, d2);
     if (p.pml) {
       const int sz = slab_index(p.slab[2], k);
       if (sz >= 0) d2 = pml_term<C>(d2, p.psiH[0][1] + (long long)i * p.slab[2].n + sz, p.bH[2][k], p.cH[2][k], p.rkH[2][k]);
     }
-    st<T, C>(p.H[0] + c, fmaC(p.Dbs, d2, ld<T, C>(p.H[0] + c)));
+    nhx = fmaC(p.Dbs, d2, hx);
   }
   // Hz: i < Nx-1; Hz -= Db*(curl1/kappa + psi1), curl1 = dEy/dx (x profile)
-  if (i < p.Nx - 1) {
-    C d1 = ld<T, C>(p.E[1] + c + p.si) - ey;
+  if (uz) {
+    C d1 = ey_i - ey;
     if (!UNI) d1 *= p.rd[0];
     if (p.tfsf) tfsf_apply<C>(p.setsH[2][0], p.tab, i, 0, k, d1);
     if (p.pml) {
       const int sx = slab_index(p.slab[0], i);
       if (sx >= 0) d1 = pml_term<C>(d1, p.psiH[2][0] + (long long)sx * p.Nzp + k, p.bH[0][i], p.cH[0][i], p.rkH[0][i]);
     }
-    st<T, C>(p.H[2] + c, fmaC(-p.Dbs, d1, ld<T, C>(p.H[2] + c)));
+    nhz = fmaC(-p.Dbs, d1, hz);
   }
+  if (ux) st<T, C>(p.H[0] + c, nhx);
+  if (uz) st<T, C>(p.H[2] + c, nhz);
 }
 
 template <class T, class C, bool UNI>
@@ -397,32 +406,31 @@ __global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
 // (vfield.cc:376-381), so the other cells add Cb*0 and are skipped here.
 template <class T, class C, bool UNI>
 __device__ __forceinline__ unsigned long long e_cell_2d(const StepParams<T, C>& p, const int i, const int k) {
-  unsigned long long mbits = 0ull;
-  {
-    const long long c = (long long)i * p.si + k;
-    C eyn;
-    if (i >= 1 && i < p.Nx - 1 && k >= 1 && k < p.Nz - 1) {
-      C d1 = ld<T, C>(p.H[0] + c) - ld<T, C>(p.H[0] + c - 1);     // dHx/dz (z profile)
-      C d2 = ld<T, C>(p.H[2] + c) - ld<T, C>(p.H[2] + c - p.si);  // dHz/dx (x profile)
-      if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
-      if (p.tfsf) {
-        tfsf_apply<C>(p.setsE[1][0], p.tab, i, 0, k, d1);
-        tfsf_apply<C>(p.setsE[1][1], p.tab, i, 0, k, d2);
-      }
-      if (p.pml) {
-        const int sz = slab_index(p.slab[2], k), sx = slab_index(p.slab[0], i);
-        if (sz >= 0) d1 = pml_term<C>(d1, p.psiE[1][0] + (long long)i * p.slab[2].n + sz, p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
-        if (sx >= 0) d2 = pml_term<C>(d2, p.psiE[1][1] + (long long)sx * p.Nzp + k, p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
-      }
-      eyn = fmaC(p.Cbs[1][c], d1 - d2, ld<T, C>(p.E[1] + c));
-      st<T, C>(p.E[1] + c, eyn);
-    } else {
-      eyn = ld<T, C>(p.E[1] + c);
+  const long long c = (long long)i * p.si + k;
+  const bool u = (i >= 1 && i < p.Nx - 1 && k >= 1 && k < p.Nz - 1);
+  const C ey = ld<T, C>(p.E[1] + c);
+  const C hx = u ? ld<T, C>(p.H[0] + c) : C(0), hx_k = u ? ld<T, C>(p.H[0] + c - 1) : C(0);
+  const C hz = u ? ld<T, C>(p.H[2] + c) : C(0), hz_i = u ? ld<T, C>(p.H[2] + c - p.si) : C(0);
+  const C cb = u ? p.Cbs[1][c] : C(0);
+  C eyn = ey;
+  if (u) {
+    C d1 = hx - hx_k;  // dHx/dz (z profile)
+    C d2 = hz - hz_i;  // dHz/dx (x profile)
+    if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
+    if (p.tfsf) {
+      tfsf_apply<C>(p.setsE[1][0], p.tab, i, 0, k, d1);
+      tfsf_apply<C>(p.setsE[1][1], p.tab, i, 0, k, d2);
     }
-    // local_max = max(Ey*Ey) over the whole Ey array (two_dim_pml.cc:181)
-    if (p.max_slot) mbits = e2_bits(eyn * eyn);
+    if (p.pml) {
+      const int sz = slab_index(p.slab[2], k), sx = slab_index(p.slab[0], i);
+      if (sz >= 0) d1 = pml_term<C>(d1, p.psiE[1][0] + (long long)i * p.slab[2].n + sz, p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
+      if (sx >= 0) d2 = pml_term<C>(d2, p.psiE[1][1] + (long long)sx * p.Nzp + k, p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
+    }
+    eyn = fmaC(cb, d1 - d2, ey);
+    st<T, C>(p.E[1] + c, eyn);
   }
-  return mbits;
+  // local_max = max(Ey*Ey) over the whole Ey array (two_dim_pml.cc:181)
+  return p.max_slot ? e2_bits(eyn * eyn) : 0ull;
 }
 
 template <class T, class C, bool UNI>

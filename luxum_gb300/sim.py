@@ -28,6 +28,15 @@ def params(**kw) -> Params:
     return p
 
 
+def device_bytes(p: Params) -> int:
+    """Device memory a handle for p would hold after creation (host-only estimate)."""
+    n = C.c_size_t()
+    st = _ffi.lib().lx_params_device_bytes(C.byref(p), C.byref(n))
+    if st:
+        raise LuxumError(st, _ffi.lib().lx_last_error(None).decode())
+    return n.value
+
+
 def read_yaml(path: str) -> Params:
     """Parses a Luxum parameters.yaml (reader::readYAML + checkData)."""
     p = Params()

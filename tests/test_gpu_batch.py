@@ -79,3 +79,16 @@ def test_batch_rejects_mixed_precision(engine):
     batch.add(a)
     with pytest.raises(LuxumError):
         batch.add(b)
+
+
+@pytest.mark.parametrize("name", sorted(cases.CASES))
+def test_device_bytes_estimate(engine, name):
+    """lx_params_device_bytes (host-only) agrees with what a created handle holds."""
+    from luxum_gb300 import Sim, device_bytes
+
+    p, steps, boxes = cases.build(name)
+    est = device_bytes(p)
+    s = Sim(p)
+    held = s.info()["device_bytes"]
+    assert 0.9 * held <= est <= 1.1 * held + 4096, (est, held)
+    s.close()
