@@ -410,6 +410,85 @@ def bench_serve(args):
     batch.close()
 
 
+PHC = dict(nx=512, ny=512, nz=128, steps=4000, cpml=20, period=40, rod=16, eps=12.0)
+PHC_OMEGA = 2 * np.pi * np.linspace(2.0e9, 3.6e9, 64)
+
+
+def phc_sim(precision: int):
+    """Photonic-crystal waveguide: square eps_r 12 rods (16x16 cells, period 40, full height) with
+    the row nearest mid-y removed; CPML 20; Gaussian-pulsed sine on Ez at the defect entrance
+    (omega 1.76e10 rad/s = 2.8 GHz, width 159 steps, centred at step 480); FP64 DFT planes
+    (64 frequencies, 2.0-3.6 GHz) across the guide at x = 40 (input) and x = 470 (output)."""
+    from luxum_gb300 import Sim, params
+
+    c = PHC
+    p = params(isPlanar=0, Nx=c["nx"], Ny=c["ny"], Nz=c["nz"], dx=1e-3, dy=1e-3, dz=1e-3, S=0.5,
+               num_timesteps=c["steps"], usePML=1, d_pml=c["cpml"] * 1e-3, sigma=0.65, sigma_m=3.0, kappa=5.0,
+               a_max=0.05, a_m=1.0, cpml_mode=1, usePS=1, source_kind=1, amp_source=1.0,
+               omega_source=2 * np.pi * 2.8e9, src_t0=480.0, src_tw=159.0, precision=precision)
+    centres = [20 + c["period"] * m for m in range(13)]
+    defect = min(centres, key=lambda y: abs(y - c["ny"] // 2))
+    p.Nx_source, p.Ny_source, p.Nz_source = c["cpml"] + 4, defect, c["nz"] // 2
+    s = Sim(p)
+    h = c["rod"] // 2
+    for xc in centres:
+        for yc in centres:
+            if yc == defect:
+                continue
+            s.set_eps_box((xc - h, yc - h, 0), (xc + h, yc + h, c["nz"]), c["eps"])
+    planes = (s.add_dft_plane(0, 40, PHC_OMEGA, every=5), s.add_dft_plane(0, 470, PHC_OMEGA, every=5))
+    return s, planes
+
+
+def bench_phc(args):
+    """--config phc: the waveguide run in FP64, FP32 and FP16 storage; errors against FP64."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    c = PHC
+    cells = c["nx"] * c["ny"] * c["nz"]
+    out = {}
+    ref = None
+    for prec, name in ((0, "fp64"), (1, "fp32"), (2, "fp16_storage")):
+        s, (pin, pout) = phc_sim(prec)
+        s.step(1)  # first touch
+        s.reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.step(c["steps"])
+        s.sync()
+        dt = time.perf_counter() - t0
+        fin, fout = s.dft_flux(pin), s.dft_flux(pout)
+        T = fout / np.where(np.abs(fin) > 0, fin, np.nan)
+        fields = [s.field(k) for k in range(6)]
+        entry = {"value": cells * c["steps"] / dt / 1e9, "unit": UNIT, "seconds": dt}
+        if ref is None:
+            ref = (fields, T, fin, fout)
+            entry["transmission"] = {"f_ghz": (PHC_OMEGA[::8] / 2 / np.pi / 1e9).round(3).tolist(),
+                                     "T": np.round(T[::8], 4).tolist()}
+        else:
+            errs = {}
+            for grp, comps in (("E", (0, 1, 2)), ("H", (3, 4, 5))):
+                num = sum(float(np.linalg.norm(fields[k] - ref[0][k])) ** 2 for k in comps)
+                den = sum(float(np.linalg.norm(ref[0][k])) ** 2 for k in comps)
+                errs[grp] = (num / den) ** 0.5
+            entry["field_rel_l2_vs_fp64"] = errs
+            entry["T_max_abs_err_vs_fp64"] = float(np.nanmax(np.abs(T - ref[1])))
+            entry["T_rel_l2_vs_fp64"] = float(np.sqrt(np.nansum((T - ref[1]) ** 2) / np.nansum(ref[1] ** 2)))
+            entry["flux_out_rel_l2_vs_fp64"] = float(np.linalg.norm(fout - ref[3]) / np.linalg.norm(ref[3]))
+            entry["speedup_vs_fp64"] = out["fp64"]["seconds"] / dt
+        out[name] = entry
+        del fields
+        s.close()
+    line = {"config": {"workload": "3-D photonic-crystal waveguide 512x512x128, eps_r 12 rods 16x16 cells period 40 "
+                                   "with a one-row line defect, CPML 20, pulsed Ez point source, 4000 steps; FP64 DFT "
+                                   "transmission (64 frequencies 2.0-3.6 GHz, planes x=40 and x=470)"},
+            "metric": "Gcell-updates/s and error vs FP64 per precision", "results": out}
+    print(json.dumps(line), flush=True)
+
+
 def dist_setup(n_gpus: int):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -477,7 +556,7 @@ def main():
                     help="run the N^3 profiling case instead of the benchmark (for ncu)")
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--precision", type=int, default=0, help="profiling case precision: 0 fp64, 1 fp32, 2 fp16")
-    ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "serve"],
+    ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "serve", "phc"],
                     help="drop-in: the headline 256^3 FP64 workload; batch: 256 uneven planar simulations")
     ap.add_argument("--batch-sims", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=3000)
@@ -492,6 +571,8 @@ def main():
         return bench_batch(args)
     if args.config == "serve":
         return bench_serve(args)
+    if args.config == "phc":
+        return bench_phc(args)
     if args.profile:
         return profile_case(args.profile, args.profile_steps, args.precision)
     if args.warmup < 3:

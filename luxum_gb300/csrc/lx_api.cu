@@ -1085,6 +1085,17 @@ static lx::StepParams<T, C> step_params(lx_sim* s) {
     }
   p.tfsf = s->tfsf && s->tab_total > 0;
   p.tab = (const C*)s->tab;
+  // plane lists of the block skip test: per axis, the planes any active set of that half step
+  // sits on (two per axis: the low and high face)
+  for (int a = 0; a < 3; a++)
+    for (int q = 0; q < 2; q++) p.planesH[a][q] = p.planesE[a][q] = -2;
+  for (int c = 0; c < 3; c++)
+    for (int q = 0; q < 2; q++) {
+      const lx::PatchSet& h = s->setsH[c][q];
+      const lx::PatchSet& e = s->setsE[c][q];
+      if (h.active) { p.planesH[h.axis][0] = h.plane[0]; p.planesH[h.axis][1] = h.plane[1]; }
+      if (e.active) { p.planesE[e.axis][0] = e.plane[0]; p.planesE[e.axis][1] = e.plane[1]; }
+    }
   return p;
 }
 
@@ -1501,10 +1512,10 @@ static lx_status batch_rebuild(lx_batch* b) {
       sp.etotal = nullptr;
       ps.push_back(sp);
       if (s->planar) {
-        for (int i0 = 0; i0 < s->Nx; i0 += 8)
+        for (int i0 = 0; i0 < s->Nx; i0 += 8 * lx::kMarch)
           for (int k0 = 0; k0 < s->Nz; k0 += 32) tiles.push_back({(int)li, i0, 0, k0});
       } else {
-        for (int i = 0; i < s->Nx; i++)
+        for (int i = 0; i < s->Nx; i += lx::kMarch)
           for (int j0 = 0; j0 < s->Ny; j0 += 8)
             for (int k0 = 0; k0 < s->Nz; k0 += 32) tiles.push_back({(int)li, i, j0, k0});
       }

@@ -24,6 +24,8 @@ namespace lx {
 
 constexpr int kMaxProbes = 64;
 constexpr int kMaxDftFreq = 256;
+// Cells each thread of an update kernel walks through along x (3-D planes; planar: rows 8 apart).
+constexpr int kMarch = 4;
 
 // Packed CPML slab along one axis.
 struct Slab {
@@ -101,6 +103,8 @@ struct StepParams {
   C* psiE[3][2];
   // TF/SF
   int tfsf;
+  int planesH[3][2];     // per axis, the planes any H-update set uses (-2 when none): block skip test
+  int planesE[3][2];
   PatchSet setsH[3][2];  // [component][part]
   PatchSet setsE[3][2];
   const C* tab;
@@ -116,10 +120,11 @@ struct ProbeParams {
   const int* ijk;   // device array [nprobes][3]
 };
 
-// One tile of a batched launch: 32 (z) x 8 (y, or x in planar grids) cells of one simulation.
+// One tile of a batched launch: 32 (z) x 8 (y) x kMarch (x) cells of one 3-D simulation, or
+// 32 (z) x 8*kMarch (x) cells of a planar one.
 struct Tile {
   int sim;  // index into the batch's parameter array
-  int a;    // 3-D: x plane; planar: first x index
+  int a;    // 3-D: first x plane; planar: first x index
   int b;    // 3-D: first y index
   int c;    // first z index
 };

@@ -65,6 +65,19 @@ __device__ __forceinline__ void tfsf_apply(const PatchSet& ps, const C* tab, int
   if (h1) d = d + tab[ps.tab + ps.plane_len + off];
 }
 
+// Whether a block's tile [i0,i0+ni) x [j0,j0+nj) x [k0,k0+nk) meets any TF/SF plane of the
+// given plane lists; blocks that do not skip every per-cell plane test.
+__device__ __forceinline__ bool tile_meets_planes(const int (&pl)[3][2], int i0, int ni, int j0, int nj, int k0, int nk) {
+  bool t = false;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    t |= (unsigned)(pl[0][q] - i0) < (unsigned)ni;
+    t |= (unsigned)(pl[1][q] - j0) < (unsigned)nj;
+    t |= (unsigned)(pl[2][q] - k0) < (unsigned)nk;
+  }
+  return t;
+}
+
 // psi = b*psi + c*curl; returns curl/kappa + psi (reference: three_dim_pml.cc:186-188).
 template <class C>
 __device__ __forceinline__ C pml_term(C d, C* psi, C b, C cc, C rk) {
@@ -207,7 +220,8 @@ __device__ __forceinline__ unsigned long long e2_bits(float v) {
 
 // H half-step over cell (i,j,k) for Hx, Hy, Hz (three_dim_pml.cc:176-213, three_dim.cc:101-132).
 template <class T, class C, bool UNI>
-__device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k) {
+__device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k,
+                                          const bool tf) {
   const long long c = (long long)i * p.si + (long long)j * p.sj + k;
   const bool ux = (j < p.Ny - 1 && k < p.Nz - 1), uy = (i < p.Nx - 1 && k < p.Nz - 1), uz = (i < p.Nx - 1 && j < p.Ny - 1);
   // Every load is issued before any store: the field arrays may alias as far as the compiler
@@ -229,7 +243,7 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
   if (ux) {
     C d1 = ez_j - ez, d2 = ey_k - ey;
     if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
-    if (p.tfsf) {
+    if (tf) {
       tfsf_apply<C>(p.setsH[0][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsH[0][1], p.tab, i, j, k, d2);
     }
@@ -241,7 +255,7 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
   if (uy) {
     C d1 = ex_k - ex, d2 = ez_i - ez;
     if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
-    if (p.tfsf) {
+    if (tf) {
       tfsf_apply<C>(p.setsH[1][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsH[1][1], p.tab, i, j, k, d2);
     }
@@ -253,7 +267,7 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
   if (uz) {
     C d1 = ey_i - ey, d2 = ex_j - ex;
     if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
-    if (p.tfsf) {
+    if (tf) {
       tfsf_apply<C>(p.setsH[2][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsH[2][1], p.tab, i, j, k, d2);
     }
@@ -266,24 +280,36 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
   if (uz) st<T, C>(p.H[2] + c, nhz);
 }
 
-template <class T, class C, bool UNI>
+// Each block owns a 32 (z) x 8 (y) column of cells over kMarch consecutive x planes; each
+// thread walks its column through the planes, so index set-up and the TF/SF tile test are
+// paid once per kMarch cells.
+template <class T, class C, bool UNI, int M>
 __global__ void __launch_bounds__(256) h_kernel_3d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
-  const int i = blockIdx.z;
-  if (k < p.Nz && j < p.Ny) h_cell_3d<T, C, UNI>(p, i, j, k);
+  const int i0 = blockIdx.z * M;
+  if (k >= p.Nz || j >= p.Ny) return;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, M, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
+  if constexpr (M == 1) {
+    h_cell_3d<T, C, UNI>(p, i0, j, k, tf);
+  } else {
+    const int i1 = min(i0 + M, p.Nx);
+#pragma unroll 1
+    for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI>(p, i, j, k, tf);
+  }
 }
 
 // E half-step over cell (i,j,k) for Ex, Ey, Ez (three_dim_pml.cc:218-276, three_dim.cc:134-189).
 // Only cells where the reference's H-curl is computed (vfield.cc:241-269: the transverse
 // index in [1, N-2]) change; on the PEC walls the reference adds Cb*0 and psi stays 0.
 // Returns the bit pattern of this cell's |E|^2 when monitoring (0 otherwise).
-template <class T, class C, bool UNI>
-__device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k) {
+template <class T, class C, bool UNI, bool MON>
+__device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k,
+                                                        const bool tf) {
   const long long c = (long long)i * p.si + (long long)j * p.sj + k;
   const bool ii = (i >= 1 && i < p.Nx - 1), jj = (j >= 1 && j < p.Ny - 1), kk = (k >= 1 && k < p.Nz - 1);
   const bool ux = (i < p.Nx - 1 && jj && kk), uy = (ii && j < p.Ny - 1 && kk), uz = (ii && jj && k < p.Nz - 1);
-  const bool mon = (p.max_slot != nullptr || p.etotal != nullptr) && i < p.Nx - 1 && j < p.Ny - 1 && k < p.Nz - 1;
+  const bool mon = MON && i < p.Nx - 1 && j < p.Ny - 1 && k < p.Nz - 1;
   // all loads first (see h_cell_3d)
   const C hx = ld<T, C>(p.H[0] + c), hy = ld<T, C>(p.H[1] + c), hz = ld<T, C>(p.H[2] + c);
   const C hz_j = ux ? ld<T, C>(p.H[2] + c - p.sj) : C(0), hy_k = ux ? ld<T, C>(p.H[1] + c - 1) : C(0);
@@ -303,7 +329,7 @@ __device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& 
   if (ux) {
     C d1 = hz - hz_j, d2 = hy - hy_k;
     if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
-    if (p.tfsf) {
+    if (tf) {
       tfsf_apply<C>(p.setsE[0][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsE[0][1], p.tab, i, j, k, d2);
     }
@@ -315,7 +341,7 @@ __device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& 
   if (uy) {
     C d1 = hx - hx_k, d2 = hz - hz_i;
     if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
-    if (p.tfsf) {
+    if (tf) {
       tfsf_apply<C>(p.setsE[1][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsE[1][1], p.tab, i, j, k, d2);
     }
@@ -327,7 +353,7 @@ __device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& 
   if (uz) {
     C d1 = hy - hy_i, d2 = hx - hx_j;
     if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
-    if (p.tfsf) {
+    if (tf) {
       tfsf_apply<C>(p.setsE[2][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsE[2][1], p.tab, i, j, k, d2);
     }
@@ -348,20 +374,33 @@ __device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& 
   return mbits;
 }
 
-template <class T, class C, bool UNI>
+template <class T, class C, bool UNI, bool MON, int M>
 __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
-  const int i = blockIdx.z;
-  const unsigned long long mbits = (k < p.Nz && j < p.Ny) ? e_cell_3d<T, C, UNI>(p, i, j, k) : 0ull;
-  if (p.max_slot) block_max_atomic(mbits, p.max_slot);
+  const int i0 = blockIdx.z * M;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, M, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
+  unsigned long long mbits = 0ull;
+  if (k < p.Nz && j < p.Ny) {
+    if constexpr (M == 1) {
+      mbits = e_cell_3d<T, C, UNI, MON>(p, i0, j, k, tf);
+    } else {
+      const int i1 = min(i0 + M, p.Nx);
+#pragma unroll 1
+      for (int i = i0; i < i1; ++i) {
+        const unsigned long long b = e_cell_3d<T, C, UNI, MON>(p, i, j, k, tf);
+        mbits = b > mbits ? b : mbits;
+      }
+    }
+  }
+  if (MON && p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
 // ------------------------------------------------------------------ planar kernels
 
 // Planar H half-step (x-z plane, Ny = 1): Hx and Hz (two_dim_pml.cc:144-162, two_dim.cc:95-111).
 template <class T, class C, bool UNI>
-__device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i, const int k) {
+__device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i, const int k, const bool tf) {
   const long long c = (long long)i * p.si + k;
   const bool ux = k < p.Nz - 1, uz = i < p.Nx - 1;
   const C ey = ld<T, C>(p.E[1] + c);
@@ -372,7 +411,7 @@ __device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i
   if (ux) {
     C d2 = ey_k - ey;
     if (!UNI) d2 *= p.rd[2];
-    if (p.tfsf) tfsf_apply<C>(p.setsH[0][1], p.tab, i, 0, k, d2);
+    if (tf) tfsf_apply<C>(p.setsH[0][1], p.tab, i, 0, k, d2);
     if (p.pml) {
       const int sz = slab_index(p.slab[2], k);
       if (sz >= 0) d2 = pml_term<C>(d2, p.psiH[0][1] + (long long)i * p.slab[2].n + sz, p.bH[2][k], p.cH[2][k], p.rkH[2][k]);
@@ -383,7 +422,7 @@ __device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i
   if (uz) {
     C d1 = ey_i - ey;
     if (!UNI) d1 *= p.rd[0];
-    if (p.tfsf) tfsf_apply<C>(p.setsH[2][0], p.tab, i, 0, k, d1);
+    if (tf) tfsf_apply<C>(p.setsH[2][0], p.tab, i, 0, k, d1);
     if (p.pml) {
       const int sx = slab_index(p.slab[0], i);
       if (sx >= 0) d1 = pml_term<C>(d1, p.psiH[2][0] + (long long)sx * p.Nzp + k, p.bH[0][i], p.cH[0][i], p.rkH[0][i]);
@@ -394,21 +433,29 @@ __device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i
   if (uz) st<T, C>(p.H[2] + c, nhz);
 }
 
-template <class T, class C, bool UNI>
+// Each block owns 32 (z) x 8*kMarch (x) cells; thread row r handles x rows r, r+8, ...
+template <class T, class C, bool UNI, int M>
 __global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
-  const int i = blockIdx.y * 8 + threadIdx.y;
-  if (k < p.Nz && i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k);
+  const int ib = blockIdx.y * 8 * M;
+  if (k >= p.Nz) return;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, ib, 8 * M, 0, 1, blockIdx.x * 32, 32);
+#pragma unroll 1
+  for (int r = 0; r < M; ++r) {
+    const int i = ib + threadIdx.y + 8 * r;
+    if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
+  }
 }
 
 // Planar E half-step: Ey (two_dim_pml.cc:164-181, two_dim.cc:113-128).  The reference loop
 // covers i < Nx-1, k < Nz-1, but its H-curl is only computed for i, k in [1, N-2]
 // (vfield.cc:376-381), so the other cells add Cb*0 and are skipped here.
-template <class T, class C, bool UNI>
-__device__ __forceinline__ unsigned long long e_cell_2d(const StepParams<T, C>& p, const int i, const int k) {
+template <class T, class C, bool UNI, bool MON>
+__device__ __forceinline__ unsigned long long e_cell_2d(const StepParams<T, C>& p, const int i, const int k,
+                                                        const bool tf) {
   const long long c = (long long)i * p.si + k;
   const bool u = (i >= 1 && i < p.Nx - 1 && k >= 1 && k < p.Nz - 1);
-  const C ey = ld<T, C>(p.E[1] + c);
+  const C ey = (u || MON) ? ld<T, C>(p.E[1] + c) : C(0);
   const C hx = u ? ld<T, C>(p.H[0] + c) : C(0), hx_k = u ? ld<T, C>(p.H[0] + c - 1) : C(0);
   const C hz = u ? ld<T, C>(p.H[2] + c) : C(0), hz_i = u ? ld<T, C>(p.H[2] + c - p.si) : C(0);
   const C cb = u ? p.Cbs[1][c] : C(0);
@@ -417,7 +464,7 @@ __device__ __forceinline__ unsigned long long e_cell_2d(const StepParams<T, C>& 
     C d1 = hx - hx_k;  // dHx/dz (z profile)
     C d2 = hz - hz_i;  // dHz/dx (x profile)
     if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
-    if (p.tfsf) {
+    if (tf) {
       tfsf_apply<C>(p.setsE[1][0], p.tab, i, 0, k, d1);
       tfsf_apply<C>(p.setsE[1][1], p.tab, i, 0, k, d2);
     }
@@ -430,15 +477,26 @@ __device__ __forceinline__ unsigned long long e_cell_2d(const StepParams<T, C>& 
     st<T, C>(p.E[1] + c, eyn);
   }
   // local_max = max(Ey*Ey) over the whole Ey array (two_dim_pml.cc:181)
-  return p.max_slot ? e2_bits(eyn * eyn) : 0ull;
+  return MON ? e2_bits(eyn * eyn) : 0ull;
 }
 
-template <class T, class C, bool UNI>
+template <class T, class C, bool UNI, bool MON, int M>
 __global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
-  const int i = blockIdx.y * 8 + threadIdx.y;
-  const unsigned long long mbits = (k < p.Nz && i < p.Nx) ? e_cell_2d<T, C, UNI>(p, i, k) : 0ull;
-  if (p.max_slot) block_max_atomic(mbits, p.max_slot);
+  const int ib = blockIdx.y * 8 * M;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, ib, 8 * M, 0, 1, blockIdx.x * 32, 32);
+  unsigned long long mbits = 0ull;
+  if (k < p.Nz) {
+#pragma unroll 1
+    for (int r = 0; r < M; ++r) {
+      const int i = ib + threadIdx.y + 8 * r;
+      if (i < p.Nx) {
+        const unsigned long long b = e_cell_2d<T, C, UNI, MON>(p, i, k, tf);
+        mbits = b > mbits ? b : mbits;
+      }
+    }
+  }
+  if (MON && p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
 // ------------------------------------------------------------------ batched update kernels
@@ -448,16 +506,29 @@ template <class T, class C, bool UNI>
 __global__ void __launch_bounds__(256) h_batch_3d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
   const Tile tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.sim];
-  const int k = tl.c + threadIdx.x, j = tl.b + threadIdx.y, i = tl.a;
-  if (k < p.Nz && j < p.Ny) h_cell_3d<T, C, UNI>(p, i, j, k);
+  const int k = tl.c + threadIdx.x, j = tl.b + threadIdx.y, i0 = tl.a;
+  if (k >= p.Nz || j >= p.Ny) return;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, kMarch, tl.b, 8, tl.c, 32);
+  const int i1 = min(i0 + kMarch, p.Nx);
+#pragma unroll 1
+  for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI>(p, i, j, k, tf);
 }
 
 template <class T, class C, bool UNI>
 __global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
   const Tile tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.sim];
-  const int k = tl.c + threadIdx.x, j = tl.b + threadIdx.y, i = tl.a;
-  const unsigned long long mbits = (k < p.Nz && j < p.Ny) ? e_cell_3d<T, C, UNI>(p, i, j, k) : 0ull;
+  const int k = tl.c + threadIdx.x, j = tl.b + threadIdx.y, i0 = tl.a;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, kMarch, tl.b, 8, tl.c, 32);
+  unsigned long long mbits = 0ull;
+  if (k < p.Nz && j < p.Ny) {
+    const int i1 = min(i0 + kMarch, p.Nx);
+#pragma unroll 1
+    for (int i = i0; i < i1; ++i) {
+      const unsigned long long b = e_cell_3d<T, C, UNI, true>(p, i, j, k, tf);
+      mbits = b > mbits ? b : mbits;
+    }
+  }
   if (p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
@@ -465,16 +536,33 @@ template <class T, class C, bool UNI>
 __global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
   const Tile tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.sim];
-  const int k = tl.c + threadIdx.x, i = tl.a + threadIdx.y;
-  if (k < p.Nz && i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k);
+  const int k = tl.c + threadIdx.x;
+  if (k >= p.Nz) return;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, tl.a, 8 * kMarch, 0, 1, tl.c, 32);
+#pragma unroll 1
+  for (int r = 0; r < kMarch; ++r) {
+    const int i = tl.a + threadIdx.y + 8 * r;
+    if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
+  }
 }
 
 template <class T, class C, bool UNI>
 __global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
   const Tile tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.sim];
-  const int k = tl.c + threadIdx.x, i = tl.a + threadIdx.y;
-  const unsigned long long mbits = (k < p.Nz && i < p.Nx) ? e_cell_2d<T, C, UNI>(p, i, k) : 0ull;
+  const int k = tl.c + threadIdx.x;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, tl.a, 8 * kMarch, 0, 1, tl.c, 32);
+  unsigned long long mbits = 0ull;
+  if (k < p.Nz) {
+#pragma unroll 1
+    for (int r = 0; r < kMarch; ++r) {
+      const int i = tl.a + threadIdx.y + 8 * r;
+      if (i < p.Nx) {
+        const unsigned long long b = e_cell_2d<T, C, UNI, true>(p, i, k, tf);
+        mbits = b > mbits ? b : mbits;
+      }
+    }
+  }
   if (p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
@@ -640,24 +728,34 @@ cudaError_t launch_prologue(const PrologueParams& p, cudaStream_t s) {
 
 template <class T, class C>
 cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bool h_half, cudaStream_t s) {
+  // single simulations: one cell per thread (their parameters sit in the constant bank, and
+  // walking several cells raises register use past what pays off)
+  constexpr int M = 1;
   dim3 block(32, 8);
+  const bool mon = p.max_slot || p.etotal;
   if (planar) {
-    dim3 grid((p.Nz + 31) / 32, (p.Nx + 7) / 8, 1);
+    dim3 grid((p.Nz + 31) / 32, (p.Nx + 8 * M - 1) / (8 * M), 1);
     if (h_half) {
-      if (uniform) h_kernel_2d<T, C, true><<<grid, block, 0, s>>>(p);
-      else h_kernel_2d<T, C, false><<<grid, block, 0, s>>>(p);
+      if (uniform) h_kernel_2d<T, C, true, M><<<grid, block, 0, s>>>(p);
+      else h_kernel_2d<T, C, false, M><<<grid, block, 0, s>>>(p);
+    } else if (mon) {
+      if (uniform) e_kernel_2d<T, C, true, true, M><<<grid, block, 0, s>>>(p);
+      else e_kernel_2d<T, C, false, true, M><<<grid, block, 0, s>>>(p);
     } else {
-      if (uniform) e_kernel_2d<T, C, true><<<grid, block, 0, s>>>(p);
-      else e_kernel_2d<T, C, false><<<grid, block, 0, s>>>(p);
+      if (uniform) e_kernel_2d<T, C, true, false, M><<<grid, block, 0, s>>>(p);
+      else e_kernel_2d<T, C, false, false, M><<<grid, block, 0, s>>>(p);
     }
   } else {
-    dim3 grid((p.Nz + 31) / 32, (p.Ny + 7) / 8, p.Nx);
+    dim3 grid((p.Nz + 31) / 32, (p.Ny + 7) / 8, (p.Nx + M - 1) / M);
     if (h_half) {
-      if (uniform) h_kernel_3d<T, C, true><<<grid, block, 0, s>>>(p);
-      else h_kernel_3d<T, C, false><<<grid, block, 0, s>>>(p);
+      if (uniform) h_kernel_3d<T, C, true, M><<<grid, block, 0, s>>>(p);
+      else h_kernel_3d<T, C, false, M><<<grid, block, 0, s>>>(p);
+    } else if (mon) {
+      if (uniform) e_kernel_3d<T, C, true, true, M><<<grid, block, 0, s>>>(p);
+      else e_kernel_3d<T, C, false, true, M><<<grid, block, 0, s>>>(p);
     } else {
-      if (uniform) e_kernel_3d<T, C, true><<<grid, block, 0, s>>>(p);
-      else e_kernel_3d<T, C, false><<<grid, block, 0, s>>>(p);
+      if (uniform) e_kernel_3d<T, C, true, false, M><<<grid, block, 0, s>>>(p);
+      else e_kernel_3d<T, C, false, false, M><<<grid, block, 0, s>>>(p);
     }
   }
   return cudaGetLastError();
