@@ -335,79 +335,54 @@ def serve_params(req):
     return params(isPlanar=0, Nx=n, Ny=n, Nz=n, Ez_pw=1.0, **kw)
 
 
-def serve_sim(req):
-    """One request as a handle: dielectric boxes and a DFT plane 4 cells before the TF/SF box's far face."""
-    from luxum_gb300 import Sim
-
-    s = Sim(serve_params(req))
-    for lo, hi, eps in req["boxes"]:
-        s.set_eps_box(lo, hi, eps)
-    plane = s.add_dft_plane(0, req["side"] - 1 - 2 * serve_margin(req["side"]) - 4, SERVE_OMEGA, every=10)
-    return s, plane
-
-
 def bench_serve(args):
-    """--config serve: continuous batching of a Poisson request stream under an HBM budget."""
-    import collections
-
+    """--config serve: a Poisson request stream through the native server (lx_server_*):
+    continuous batching under an HBM budget, latency taken by the server's own clock."""
     import torch
 
     import __graft_entry__
 
     __graft_entry__.build()
-    from luxum_gb300 import Batch, device_bytes
+    from luxum_gb300 import LX_PREC_FP32, Server
 
     reqs = serve_requests(args.serve_requests, 5, args.serve_rate)
-    budget = args.serve_budget_gb * 1e9
-    chunk = args.serve_chunk
-    for r in reqs:
-        r["bytes"] = device_bytes(serve_params(r)) + 4 * 64 * 16 * (r["side"] ** (1 if r["planar"] else 2))
-        r["cells"] = r["side"] ** (2 if r["planar"] else 3)
-    batch = Batch(chunk=chunk)
-    queue = collections.deque(reqs)
-    active = {}
-    used = 0.0
-    lat, peak_active, peak_bytes, work = [], 0, 0.0, 0
+    srv = Server(precision=LX_PREC_FP32, chunk=args.serve_chunk, budget_bytes=args.serve_budget_gb * 1e9)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    ids = []
     with ClockSampler(0) as clk:
-        while queue or active:
-            now = time.perf_counter() - t0
-            while queue and queue[0]["arrival"] <= now and (used + queue[0]["bytes"] <= budget or not active):
-                r = queue.popleft()
-                s, plane = serve_sim(r)
-                batch.add(s)
-                active[id(s)] = (s, plane, r)
-                used += r["bytes"]
-            peak_active = max(peak_active, len(active))
-            peak_bytes = max(peak_bytes, used)
-            if not active:
-                time.sleep(max(0.0, queue[0]["arrival"] - (time.perf_counter() - t0)))
+        for r in reqs:  # submit each request at its arrival time
+            d = r["arrival"] - (time.perf_counter() - t0)
+            if d > 0:
+                time.sleep(d)
+            plane = r["side"] - 1 - 2 * serve_margin(r["side"]) - 4
+            ids.append(srv.submit(serve_params(r), SERVE_STEPS, r["boxes"], (0, plane, SERVE_OMEGA, 10)))
+        lat, work, failed = [], 0, 0
+        for rid, r in zip(ids, reqs):
+            if srv.wait(rid) != "done":
+                failed += 1
                 continue
-            batch.step(chunk)
-            for key in list(active):
-                s, plane, r = active[key]
-                if s.t >= SERVE_STEPS:
-                    flux = s.dft_flux(plane)
-                    assert np.all(np.isfinite(flux))
-                    lat.append(time.perf_counter() - t0 - r["arrival"])
-                    work += r["cells"] * SERVE_STEPS
-                    batch.remove(s)
-                    s.close()
-                    used -= r["bytes"]
-                    del active[key]
+            flux = srv.flux(rid)
+            assert np.all(np.isfinite(flux))
+            t = srv.times(rid)
+            lat.append(t[2] - t[0])
+            work += r["side"] ** (2 if r["planar"] else 3) * SERVE_STEPS
+            srv.release(rid)
         wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
     lat = np.array(lat)
-    offered = sum(r["cells"] for r in reqs) * SERVE_STEPS / reqs[-1]["arrival"] / 1e9
+    offered = sum(r["side"] ** (2 if r["planar"] else 3) for r in reqs) * SERVE_STEPS / reqs[-1]["arrival"] / 1e9
     line = {"config": {"workload": f"{len(reqs)} requests, Poisson {args.serve_rate}/s (seed 5), 80% planar 256-2048, "
                                    f"20% 3-D 64-256, 1-8 eps boxes, {SERVE_STEPS} steps FP32, FP64 DFT 64 freqs at one "
-                                   f"plane (sampled every 10 steps), budget {args.serve_budget_gb} GB, chunk {chunk}"},
+                                   f"plane (sampled every 10 steps), budget {args.serve_budget_gb} GB, chunk "
+                                   f"{args.serve_chunk}; native server (lx_server_*)"},
             "metric": "p50/p99 latency and aggregate Gcell-updates/s", "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "value": work / wall / 1e9,
-            "unit": UNIT, "offered_gcells": offered, "wall_s": wall, "completed": int(lat.size),
-            "peak_active": peak_active, "peak_budget_gb": peak_bytes / 1e9, "dtype": "f32", "clocks": clk.summary()}
+            "unit": UNIT, "offered_gcells": offered, "wall_s": wall, "completed": int(lat.size), "failed": failed,
+            "peak_running": st["peak_running"], "peak_budget_gb": st["peak_bytes_running"] / 1e9,
+            "chunks": st["chunks"], "gpu_busy_s": st["busy_seconds"], "dtype": "f32", "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
-    batch.close()
 
 
 PHC = dict(nx=512, ny=512, nz=128, steps=4000, cpml=20, period=40, rod=16, eps=12.0)
@@ -489,7 +464,10 @@ def bench_phc(args):
     print(json.dumps(line), flush=True)
 
 
-def dist_setup(n_gpus: int):
+def dist_setup(n_gpus: int, backend: str | None = None):
+    """Rank, world size, local rank and the process group module (None for one process).
+    Under torchrun every rank runs an independent replica of the workload: the single
+    simulation does not shard, and no collective runs on the data path."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -498,9 +476,26 @@ def dist_setup(n_gpus: int):
         import torch.distributed as dist
 
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl" if n_gpus > 1 else "gloo")
+        dist.init_process_group(backend or ("nccl" if n_gpus > 1 else "gloo"))
         pg = dist
     return rank, world, local, pg
+
+
+def rank_max(pg, x: float) -> float:
+    """Maximum of a host number over ranks (the job's time is its slowest rank's)."""
+    if not pg:
+        return x
+    import torch
+
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, world: int, ms_max: float) -> float:
+    """Whole-job throughput in G units/s: every rank's units over the slowest rank's time."""
+    return units_per_rank * world / (ms_max * 1e-3) / 1e9
 
 
 def bench_reference(args):
@@ -632,14 +627,10 @@ def main():
         sim.sync()
         e1.record(stream)
         barrier()
-    ms = e0.elapsed_time(e1)
+    ms = rank_max(pg, e0.elapsed_time(e1))
     launches = sim.counters()[0] - k0
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
     cell_updates = N ** 3 * STEPS * args.steps * world
-    value = cell_updates / (ms * 1e-3) / 1e9
+    value = job_rate(N ** 3 * STEPS * args.steps, world, ms)
 
     # ---- end to end through the public API with pinned host buffers
     Fp = []
@@ -666,11 +657,8 @@ def main():
     t_host = time.perf_counter() - t_host
     ms_e2e = max(e2.elapsed_time(e3), 1e3 * t_host)
     _, h2d1, d2h1 = sim.counters()
-    if pg:
-        t = torch.tensor([ms_e2e], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_e2e = float(t.item())
-    e2e = {"value": cell_updates / (ms_e2e * 1e-3) / 1e9, "unit": UNIT,
+    ms_e2e = rank_max(pg, ms_e2e)
+    e2e = {"value": job_rate(N ** 3 * STEPS * args.steps, world, ms_e2e), "unit": UNIT,
            "h2d_bytes_per_step": (h2d1 - h2d0) // args.steps, "d2h_bytes_per_step": (d2h1 - d2h0) // args.steps}
 
     # ---- per-kernel roofline (instrumented pass, events around each launch)
@@ -727,7 +715,7 @@ def main():
             q.sync()
             f1.record(stream)
             barrier()
-            qms = f0.elapsed_time(f1)
+            qms = rank_max(pg, f0.elapsed_time(f1))
             errs = {}
             for grp, comps in (("E", (0, 1, 2)), ("H", (3, 4, 5))):
                 num = sum(float(np.linalg.norm(q.field(c) - ref[c])) ** 2 for c in comps)

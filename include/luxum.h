@@ -249,6 +249,78 @@ LX_API lx_status lx_batch_set_chunk(lx_batch* b, int steps);
 /* Advances every member by nsteps; returns LX_ERR_BLOWUP if any member's max|E|^2 is not
  * finite afterwards (lx_last_error(NULL) names the first such member). */
 LX_API lx_status lx_batch_step(lx_batch* b, int nsteps);
+/* lx_batch_step in two halves: enqueue the steps and return at once, so the host can
+ * prepare the next members while the GPU works; lx_batch_wait completes them (monitor
+ * read-back, blow-up check).  Members must not be touched in between. */
+LX_API lx_status lx_batch_step_async(lx_batch* b, int nsteps);
+LX_API lx_status lx_batch_wait(lx_batch* b);
+
+/* ---- Serving: continuous batching of submitted simulations --------------------------
+ * No reference counterpart: the reference runs one simulation per process.  A server owns
+ * one batch and a worker thread.  Requests queue in submission order; the worker admits
+ * the head of the queue when its device memory fits the budget (or nothing is running),
+ * creates its handle, and steps every running request together in chunks (lx_batch), so
+ * requests join and leave between chunks without stopping the others.  A chunk never
+ * overshoots a request's step count.  Handles for the next requests are created while a
+ * chunk runs on the GPU.  All calls are thread-safe. */
+typedef struct lx_server lx_server;
+typedef struct lx_server_config {
+  int precision;          /* LX_PREC_* shared by every request (default FP32) */
+  int chunk;              /* steps per batch launch, captured as a CUDA graph (default 100) */
+  double budget_bytes;    /* device memory for running requests (default 0: 90% of free) */
+  int max_running;        /* 0: no limit besides the budget */
+} lx_server_config;
+LX_API void lx_server_config_init(lx_server_config* cfg);
+
+typedef struct lx_request {
+  lx_params params;       /* params.precision must equal the server's */
+  int steps;              /* time steps to run */
+  int n_boxes;            /* dielectric boxes, applied in order (lx_sim_set_eps_box) */
+  const int* boxes;       /* n_boxes x {lo[3], hi[3]} */
+  const double* box_eps;  /* n_boxes relative permittivities */
+  int dft_axis, dft_index, dft_every; /* one DFT plane (lx_sim_add_dft_plane) when nfreq > 0 */
+  int nfreq;
+  const double* omega;    /* nfreq angular frequencies */
+} lx_request;
+LX_API void lx_request_init(lx_request* r);
+
+enum { LX_REQ_QUEUED = 0, LX_REQ_RUNNING = 1, LX_REQ_DONE = 2, LX_REQ_FAILED = 3, LX_REQ_CANCELLED = 4 };
+
+typedef struct lx_server_stats {
+  long long submitted, queued, running, done, failed, cancelled;
+  double bytes_running;       /* device-memory estimate of the running requests */
+  double peak_bytes_running;
+  int peak_running;
+  double cell_updates;        /* over all chunks stepped */
+  double busy_seconds;        /* worker time with requests running */
+  long long chunks;
+} lx_server_stats;
+
+LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_server** out);
+/* Stops the worker after the chunk in flight; running and queued requests are cancelled. */
+LX_API void lx_server_destroy(lx_server* srv);
+/* Validates and copies the request (arrays included) and queues it; *id identifies it. */
+LX_API lx_status lx_server_submit(lx_server* srv, const lx_request* req, long long* id);
+LX_API lx_status lx_server_poll(lx_server* srv, long long id, int* state);
+/* Waits until the request is DONE, FAILED or CANCELLED, or timeout_s passes (< 0: no
+ * limit); *state is its state on return. */
+LX_API lx_status lx_server_wait(lx_server* srv, long long id, double timeout_s, int* state);
+/* Queued requests leave the queue; running ones leave the batch at the next chunk end. */
+LX_API lx_status lx_server_cancel(lx_server* srv, long long id);
+/* Results of a DONE request: the DFT plane's flux (lx_sim_dft_flux) and max|E|^2. */
+LX_API lx_status lx_server_flux(lx_server* srv, long long id, double* flux, int nfreq);
+LX_API lx_status lx_server_max_e2(lx_server* srv, long long id, double* out);
+/* Seconds since the server was created at which the request was submitted, started
+ * running and finished (-1 where that has not happened). */
+LX_API lx_status lx_server_times(lx_server* srv, long long id, double t[3]);
+/* Hands the DONE request's handle to the caller (who then owns and destroys it) and
+ * forgets the request. */
+LX_API lx_status lx_server_take(lx_server* srv, long long id, lx_sim** sim);
+/* Forgets a finished, failed or cancelled request and frees its handle. */
+LX_API lx_status lx_server_release(lx_server* srv, long long id);
+/* Why a request FAILED ("" otherwise); valid until the request is released. */
+LX_API const char* lx_server_error(lx_server* srv, long long id);
+LX_API lx_status lx_server_stats_get(lx_server* srv, lx_server_stats* st);
 
 /* Launch all device work of the handle on this CUDA stream (cudaStream_t) instead of its
  * own.  NULL restores the handle's own stream. */

@@ -13,6 +13,7 @@ LIB_PATH = PKG / "libluxum.so"
 
 LX_OK, LX_ERR_INVALID, LX_ERR_UNSUPPORTED, LX_ERR_CUDA, LX_ERR_OOM, LX_ERR_BLOWUP, LX_ERR_IO, LX_ERR_STATE = range(8)
 LX_PREC_FP64, LX_PREC_FP32, LX_PREC_FP16S = 0, 1, 2
+LX_REQ_QUEUED, LX_REQ_RUNNING, LX_REQ_DONE, LX_REQ_FAILED, LX_REQ_CANCELLED = 0, 1, 2, 3, 4
 LX_CPML_REFERENCE, LX_CPML_STANDARD = 0, 1
 LX_SRC_CW_HARD, LX_SRC_PULSE_SOFT = 0, 1
 EX, EY, EZ, HX, HY, HZ, ETOTAL = range(7)
@@ -58,6 +59,23 @@ class Params(C.Structure):
 class Info(C.Structure):
     _fields_ = [("cells", C.c_size_t), ("device_bytes", C.c_size_t), ("psi_h_entries", C.c_size_t),
                 ("psi_e_entries", C.c_size_t), ("slab", C.c_int * 3), ("uniform", C.c_int), ("field_bytes", C.c_int)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("precision", C.c_int), ("chunk", C.c_int), ("budget_bytes", C.c_double), ("max_running", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("params", Params), ("steps", C.c_int), ("n_boxes", C.c_int), ("boxes", C.POINTER(C.c_int)),
+                ("box_eps", C.POINTER(C.c_double)), ("dft_axis", C.c_int), ("dft_index", C.c_int),
+                ("dft_every", C.c_int), ("nfreq", C.c_int), ("omega", C.POINTER(C.c_double))]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("queued", C.c_longlong), ("running", C.c_longlong),
+                ("done", C.c_longlong), ("failed", C.c_longlong), ("cancelled", C.c_longlong),
+                ("bytes_running", C.c_double), ("peak_bytes_running", C.c_double), ("peak_running", C.c_int),
+                ("cell_updates", C.c_double), ("busy_seconds", C.c_double), ("chunks", C.c_longlong)]
 
 
 SNAPSHOT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int))
@@ -112,6 +130,24 @@ def declare(lib) -> None:
     _proto(lib, "lx_batch_size", C.c_int, C.c_void_p)
     _proto(lib, "lx_batch_set_chunk", C.c_int, C.c_void_p, C.c_int)
     _proto(lib, "lx_batch_step", C.c_int, C.c_void_p, C.c_int)
+    _proto(lib, "lx_batch_step_async", C.c_int, C.c_void_p, C.c_int)
+    _proto(lib, "lx_batch_wait", C.c_int, C.c_void_p)
+    srv, ll = C.c_void_p, C.c_longlong
+    _proto(lib, "lx_server_config_init", None, P(ServerConfig))
+    _proto(lib, "lx_request_init", None, P(Request))
+    _proto(lib, "lx_server_create", C.c_int, P(ServerConfig), P(C.c_void_p))
+    _proto(lib, "lx_server_destroy", None, srv)
+    _proto(lib, "lx_server_submit", C.c_int, srv, P(Request), P(ll))
+    _proto(lib, "lx_server_poll", C.c_int, srv, ll, P(C.c_int))
+    _proto(lib, "lx_server_wait", C.c_int, srv, ll, C.c_double, P(C.c_int))
+    _proto(lib, "lx_server_cancel", C.c_int, srv, ll)
+    _proto(lib, "lx_server_flux", C.c_int, srv, ll, P(C.c_double), C.c_int)
+    _proto(lib, "lx_server_max_e2", C.c_int, srv, ll, P(C.c_double))
+    _proto(lib, "lx_server_times", C.c_int, srv, ll, P(C.c_double))
+    _proto(lib, "lx_server_take", C.c_int, srv, ll, P(C.c_void_p))
+    _proto(lib, "lx_server_release", C.c_int, srv, ll)
+    _proto(lib, "lx_server_error", C.c_char_p, srv, ll)
+    _proto(lib, "lx_server_stats_get", C.c_int, srv, P(ServerStats))
     _proto(lib, "lx_host_alloc", C.c_int, C.c_size_t, P(C.c_void_p))
     _proto(lib, "lx_host_free", None, C.c_void_p)
     _proto(lib, "lx_last_error", C.c_char_p, sim)

@@ -19,7 +19,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libluxum.so"
 CLI = PKG / "luxum"
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["lx_kernels.cu", "lx_api.cu", "lx_yaml.cpp", "lx_hdf5.cpp", "lx_noalloc.cu"]
+LIB_SOURCES = ["lx_kernels.cu", "lx_api.cu", "lx_yaml.cpp", "lx_hdf5.cpp", "lx_noalloc.cu", "lx_server.cpp"]
 
 
 def nvcc() -> str:

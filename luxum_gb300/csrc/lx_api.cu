@@ -15,7 +15,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/luxum.h"
+#include "luxum.h"
 #include "lx_hdf5.h"
 #include "lx_internal.h"
 #include "lx_kernels.h"
@@ -228,6 +228,7 @@ static PatchSet mkset(const lx_sim* s, int axis, int pl0, int pl1, double pos0, 
   ps.neg = neg;
   ps.dn = dn;
   ps.hcurl = hcurl;
+  ps.scale = hcurl ? s->hscale : 1.0;
   bool empty = false;
   for (int b = 0; b < 3; b++) {
     ps.lo[b] = lo[b];
@@ -352,8 +353,20 @@ static size_t ext_n(const lx_sim* s, int c) { return (size_t)s->ext[c][0] * s->e
 
 static void stop_writer(lx_sim* s);
 
+// Completes a batch chunk in flight that this handle is a member of, before the handle's
+// own state is read, written or stepped.  A blow-up is reported by the batch's own wait and
+// shows in this handle's max|E|^2; only CUDA errors are returned here.
+extern "C" LX_API lx_status lx_batch_wait(lx_batch* b);
+extern "C" LX_API lx_status lx_batch_remove(lx_batch* b, lx_sim* s);
+static lx_status settle(lx_sim* s) {
+  if (!s->batch) return LX_OK;
+  const lx_status st = lx_batch_wait(s->batch);
+  return st == LX_ERR_BLOWUP ? LX_OK : st;
+}
+
 extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
   if (!s) return;
+  if (s->batch) lx_batch_remove(s->batch, s);
   stop_writer(s);
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->side) cudaStreamSynchronize(s->side);
@@ -374,6 +387,7 @@ extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
   for (auto& d : s->dfts) {
     dfree(d.d_omega, fs);
     dfree(d.d_acc, fs);
+    dfree(d.d_flux, fs);
   }
   if (s->own) {
     cudaStreamSynchronize(s->own);
@@ -525,7 +539,10 @@ static void setup_host(lx_sim* s, const lx_params* p) {
     pw_clip(K.r1, K.r2, 0, s->Nz - 1, &K.st[2], &K.en[2]);
   }
   s->uniform = s->planar ? (p->dx == p->dz) : (p->dx == p->dy && p->dx == p->dz);
-  s->cbs_scale = s->uniform ? 1.0 / p->dx : 1.0;
+  // FP16 storage keeps H as H * sqrt(mu0/eps0), the same order as E: stored H then stays
+  // in binary16's normal range.  Cb absorbs 1/hscale, Db and the H-curl TF/SF lines hscale.
+  s->hscale = p->precision == LX_PREC_FP16S ? pow(K.mew0 / K.epsilon0, 0.5) : 1.0;
+  s->cbs_scale = (s->uniform ? 1.0 / p->dx : 1.0) / s->hscale;
 
   // point source: check_global_limits (maxwell.cc:944-959) skips it silently off the grid
   if (p->usePS) {
@@ -647,16 +664,17 @@ static void* comp_ptr(lx_sim* s, int comp) {
 
 static lx_status gather(lx_sim* s, int comp, double* dst) {
   void* src = comp_ptr(s, comp);
+  const double mul = (comp >= LX_HX && comp <= LX_HZ) ? 1.0 / s->hscale : 1.0;
   if (comp == LX_ETOTAL) {
     // |E|^2 is kept in compute precision
-    if (s->csize == 8) CK(lx::launch_gather<double>((const double*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
-    else CK(lx::launch_gather<float>((const float*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+    if (s->csize == 8) CK(lx::launch_gather<double>((const double*)src, dst, s->ext[comp], s->Ny, s->Nzp, mul, s->stream));
+    else CK(lx::launch_gather<float>((const float*)src, dst, s->ext[comp], s->Ny, s->Nzp, mul, s->stream));
   } else if (s->prec == LX_PREC_FP64) {
-    CK(lx::launch_gather<double>((const double*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+    CK(lx::launch_gather<double>((const double*)src, dst, s->ext[comp], s->Ny, s->Nzp, mul, s->stream));
   } else if (s->prec == LX_PREC_FP32) {
-    CK(lx::launch_gather<float>((const float*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+    CK(lx::launch_gather<float>((const float*)src, dst, s->ext[comp], s->Ny, s->Nzp, mul, s->stream));
   } else {
-    CK(lx::launch_gather<__half>((const __half*)src, dst, s->ext[comp], s->Ny, s->Nzp, s->stream));
+    CK(lx::launch_gather<__half>((const __half*)src, dst, s->ext[comp], s->Ny, s->Nzp, mul, s->stream));
   }
   s->n_kernels++;
   return LX_OK;
@@ -670,6 +688,7 @@ extern "C" LX_API lx_status lx_sim_field_shape(const lx_sim* s, int comp, int sh
 
 extern "C" LX_API lx_status lx_sim_read_field(lx_sim* s, int comp, double* host, size_t n) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   if (comp < 0 || comp > LX_ETOTAL) return fail(s, LX_ERR_INVALID, "bad component");
   const size_t m = ext_n(s, comp);
   if (n != m) return fail(s, LX_ERR_INVALID, "buffer size does not match the component's staggered extent");
@@ -707,13 +726,15 @@ static lx_status upload(lx_sim* s, const double* host, size_t m) {
 
 extern "C" LX_API lx_status lx_sim_write_field(lx_sim* s, int comp, const double* host, size_t n) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   if (comp < 0 || comp > LX_HZ) return fail(s, LX_ERR_INVALID, "bad component");
   const size_t m = ext_n(s, comp);
   if (n != m) return fail(s, LX_ERR_INVALID, "buffer size does not match the component's staggered extent");
   if (m == 0) return LX_OK;
   lx_status st = upload(s, host, m);
   if (st) return st;
-  if ((st = scatter(s, comp, comp_ptr(s, comp), false, 0, 1.0, 0.0))) return st;
+  const bool hcomp = comp >= LX_HX && comp <= LX_HZ;
+  if ((st = scatter(s, comp, comp_ptr(s, comp), false, hcomp && s->hscale != 1.0 ? 1 : 0, s->hscale, 0.0))) return st;
   CK(cudaStreamSynchronize(s->stream));
   return LX_OK;
 }
@@ -784,6 +805,7 @@ extern "C" LX_API lx_status lx_sim_set_probes(lx_sim* s, const int* ijk, int npr
 
 extern "C" LX_API lx_status lx_sim_read_probes(lx_sim* s, double* host, size_t n, int* rows) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   const size_t m = (size_t)s->probe_rows * s->nprobes * 6;
   if (rows) *rows = s->probe_rows;
   if (n < m) return fail(s, LX_ERR_INVALID, "probe buffer too small");
@@ -828,6 +850,7 @@ extern "C" LX_API lx_status lx_sim_add_dft_plane(lx_sim* s, int axis, int index,
 
 extern "C" LX_API lx_status lx_sim_read_dft(lx_sim* s, int id, double* host, size_t n) {
   if (!s || !host) return fail(s, LX_ERR_INVALID, "null argument");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   if (id < 0 || id >= (int)s->dfts.size()) return fail(s, LX_ERR_INVALID, "no such DFT plane");
   const lx::DftPlane& d = s->dfts[id];
   if (n != d.n_acc) return fail(s, LX_ERR_INVALID, "buffer size must be nfreq*4*na*nb*2");
@@ -839,27 +862,26 @@ extern "C" LX_API lx_status lx_sim_read_dft(lx_sim* s, int id, double* host, siz
 
 extern "C" LX_API lx_status lx_sim_dft_flux(lx_sim* s, int id, double* flux, int nfreq) {
   if (!s || !flux) return fail(s, LX_ERR_INVALID, "null argument");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   if (id < 0 || id >= (int)s->dfts.size()) return fail(s, LX_ERR_INVALID, "no such DFT plane");
-  const lx::DftPlane& d = s->dfts[id];
+  lx::DftPlane& d = s->dfts[id];
   if (nfreq != d.nfreq) return fail(s, LX_ERR_INVALID, "nfreq does not match the plane");
-  std::vector<double> acc(d.n_acc);
-  lx_status st = lx_sim_read_dft(s, id, acc.data(), acc.size());
-  if (st) return st;
   const double sp[3] = {s->p.dx, s->p.dy, s->p.dz};
   double dA;
   if (s->planar) dA = d.axis == 0 ? sp[2] : sp[0];
   else dA = d.axis == 0 ? sp[1] * sp[2] : (d.axis == 1 ? sp[2] * sp[0] : sp[0] * sp[1]);
-  const size_t nc = (size_t)d.na * d.nb;
-  for (int f = 0; f < d.nfreq; f++) {
-    const double* e1 = &acc[((size_t)f * 4 + 0) * nc * 2];
-    const double* e2 = &acc[((size_t)f * 4 + 1) * nc * 2];
-    const double* h1 = &acc[((size_t)f * 4 + 2) * nc * 2];
-    const double* h2 = &acc[((size_t)f * 4 + 3) * nc * 2];
-    double sum = 0.0;
-    for (size_t q = 0; q < nc; q++)
-      sum += (e1[2 * q] * h2[2 * q] + e1[2 * q + 1] * h2[2 * q + 1]) - (e2[2 * q] * h1[2 * q] + e2[2 * q + 1] * h1[2 * q + 1]);
-    flux[f] = sum * dA;
+  const long long nc = (long long)d.na * d.nb;
+  if (!d.d_flux) {
+    const long long nchunk = (nc + 1023) / 1024;
+    CK(cudaMallocAsync(&d.d_flux, sizeof(double) * (d.nfreq + d.nfreq * nchunk), s->own));
+    CK(cudaStreamSynchronize(s->own));
   }
+  // deterministic on-device reduction: per-chunk partial sums, then chunks in order
+  CK(lx::launch_dft_flux(d.d_acc, d.nfreq, nc, d.d_flux + d.nfreq, dA, d.d_flux, s->stream));
+  CK(cudaMemcpyAsync(flux, d.d_flux, sizeof(double) * d.nfreq, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_kernels += 2;
+  s->n_d2h += sizeof(double) * d.nfreq;
   return LX_OK;
 }
 
@@ -1019,8 +1041,8 @@ static lx_status snapshot(lx_sim* s, int t, unsigned mask) {
   CK(cudaEventDestroy(ev));
   CK(cudaMemcpyAsync(sl.host, sl.dev, off * sizeof(double), cudaMemcpyDeviceToHost, s->side));
   CK(cudaEventRecord(sl.ev_d2h, s->side));
-  // the next gather into this slot must wait for the copy to finish
-  CK(cudaStreamWaitEvent(s->stream, sl.ev_d2h, 0));
+  // The compute stream does not wait for this copy: the slot is reused only after the
+  // writer has synchronised on ev_d2h and cleared `busy`, which the wait above checks.
   s->n_d2h += off * sizeof(double);
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1032,6 +1054,7 @@ static lx_status snapshot(lx_sim* s, int t, unsigned mask) {
 
 extern "C" LX_API lx_status lx_sim_sync(lx_sim* s) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaStreamSynchronize(s->side));
   std::unique_lock<std::mutex> lk(s->mu);
@@ -1060,7 +1083,7 @@ static lx::StepParams<T, C> step_params(lx_sim* s) {
     p.Cbs[c] = (const C*)s->Cbs[c];
   }
   const double Db = s->k.dt / s->k.mew0;  // Db arrays = dt/mew0 (two_dim_pml.cc:117, three_dim_pml.cc:130-132)
-  p.Dbs = (C)(s->uniform ? Db * (1.0 / s->p.dx) : Db);
+  p.Dbs = (C)((s->uniform ? Db * (1.0 / s->p.dx) : Db) * s->hscale);
   p.rd[0] = (C)(1.0 / s->p.dx);
   p.rd[1] = (C)(s->planar ? 0.0 : 1.0 / s->p.dy);
   p.rd[2] = (C)(1.0 / s->p.dz);
@@ -1148,6 +1171,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
   for (int c = 0; c < 6; c++)
     for (int a = 0; a < 3; a++) prb.ext[c][a] = s->ext[c][a];
   prb.ijk = s->d_probe_ijk;
+  prb.hmul = 1.0 / s->hscale;
 
   for (int q = 0; q < nsteps; q++) {
     const int t = s->t;
@@ -1194,7 +1218,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
       std::memset(&dp, 0, sizeof dp);
       dp.axis = d.axis; dp.index = d.index; dp.na = d.na; dp.nb = d.nb; dp.Ny = s->Ny; dp.Nzp = s->Nzp;
       dp.nfreq = d.nfreq; dp.t = t; dp.dt = s->k.dt; dp.weight = (double)d.every;
-      dp.omega = d.d_omega; dp.acc = d.d_acc;
+      dp.omega = d.d_omega; dp.acc = d.d_acc; dp.hmul = 1.0 / s->hscale;
       T* f4[4];
       for (int q = 0; q < 4; q++) {
         f4[q] = pf[d.comps[q]];
@@ -1235,6 +1259,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
 
 extern "C" LX_API lx_status lx_sim_step(lx_sim* s, int nsteps) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   if (nsteps < 0) return fail(s, LX_ERR_INVALID, "nsteps must be >= 0");
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1269,6 +1294,7 @@ extern "C" LX_API int lx_sim_timestep(const lx_sim* s) { return s ? s->t : -1; }
 
 extern "C" LX_API lx_status lx_sim_max_e2(lx_sim* s, double* out) {
   if (!s || !out) return fail(s, LX_ERR_INVALID, "null argument");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   *out = s->last_max;
   return LX_OK;
 }
@@ -1335,42 +1361,56 @@ struct lx_batch {
   int chunk = 100;
   bool dirty = true;
   cudaStream_t stream = nullptr;
-  struct Group {
+  struct Group {  // members sharing (planar, uniform): one update launch per half step
     bool planar = false, uniform = false;
     std::vector<int> members;  // batch-global indices
     void* d_params = nullptr;
-    lx::Tile* d_tiles = nullptr;
-    int ntiles = 0;
+    int* d_first = nullptr;
+    int4* d_tiles = nullptr;
+    int nblocks = 0;
+  };
+  struct DftClass {  // DFT planes that sample at the same batch steps
+    int every = 1, phase = 0;
+    lx::DftParams* d_planes = nullptr;
+    int* d_bfirst = nullptr;
+    int2* d_map = nullptr;
+    int nplanes = 0, nblocks = 0;
   };
   std::vector<Group> groups;
+  std::vector<DftClass> dft;
   lx::PrologueParams* d_pps = nullptr;
   int max_entries = 0;
-  bool need_prologue = false;
   int* d_ts = nullptr;
   unsigned long long* d_slots = nullptr;
-  lx::DftParams* d_dfts = nullptr;
-  int ndft = 0;
-  long long max_cells4 = 0;
+  long long step = 0;  // batch steps taken (DFT sampling classes are phases of it)
   cudaGraphExec_t exec = nullptr;
   int exec_steps = 0;
+  long long exec_base_mod = -1;
+  bool graphable = true;
   std::vector<int> host_ts;
+  int pending = 0;  // steps enqueued since the last wait
   std::string err;
 };
 
 static void batch_free_device(lx_batch* b) {
   for (auto& g : b->groups) {
     dfree(g.d_params, b->stream);
+    dfree(g.d_first, b->stream);
     dfree(g.d_tiles, b->stream);
   }
   b->groups.clear();
+  for (auto& d : b->dft) {
+    dfree(d.d_planes, b->stream);
+    dfree(d.d_bfirst, b->stream);
+    dfree(d.d_map, b->stream);
+  }
+  b->dft.clear();
   dfree(b->d_pps, b->stream);
   dfree(b->d_ts, b->stream);
   dfree(b->d_slots, b->stream);
-  dfree(b->d_dfts, b->stream);
   b->d_pps = nullptr;
   b->d_ts = nullptr;
   b->d_slots = nullptr;
-  b->d_dfts = nullptr;
   if (b->exec) cudaGraphExecDestroy(b->exec);
   b->exec = nullptr;
   b->exec_steps = 0;
@@ -1392,6 +1432,7 @@ extern "C" LX_API lx_status lx_batch_create(lx_batch** out) {
   if (!out) return fail(nullptr, LX_ERR_INVALID, "null argument");
   lx_batch* b = new (std::nothrow) lx_batch();
   if (!b) return fail(nullptr, LX_ERR_OOM, "host allocation failed");
+  keep_pool_memory();
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete b;
@@ -1404,7 +1445,9 @@ extern "C" LX_API lx_status lx_batch_create(lx_batch** out) {
 extern "C" LX_API void lx_batch_destroy(lx_batch* b) {
   if (!b) return;
   cudaStreamSynchronize(b->stream);
+  for (auto* s : b->sims) s->batch = nullptr;
   batch_free_device(b);
+  cudaStreamSynchronize(b->stream);
   cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -1420,27 +1463,32 @@ extern "C" LX_API lx_status lx_batch_set_chunk(lx_batch* b, int steps) {
   return LX_OK;
 }
 
+extern "C" LX_API lx_status lx_batch_wait(lx_batch* b);
+
 extern "C" LX_API lx_status lx_batch_add(lx_batch* b, lx_sim* s) {
   if (!b || !s) return fail(nullptr, LX_ERR_INVALID, "null argument");
-  for (auto* m : b->sims)
-    if (m == s) return bfail(b, LX_ERR_INVALID, "handle already in this batch");
+  lx_status st = lx_batch_wait(b);
+  if (st) return st;
+  if (s->batch) return bfail(b, LX_ERR_INVALID, s->batch == b ? "handle already in this batch" : "handle is in another batch");
   if (b->prec >= 0 && s->prec != b->prec) return bfail(b, LX_ERR_INVALID, "all members of a batch share one precision");
   if (!s->outputs.empty() || s->nprobes > 0)
     return bfail(b, LX_ERR_UNSUPPORTED, "batched members cannot have snapshot outputs or probes");
-  lx_status st = lx_sim_sync(s);
-  if (st) return st;
+  if ((st = lx_sim_sync(s))) return st;
   b->prec = s->prec;
   b->sims.push_back(s);
+  s->batch = b;
   b->dirty = true;
   return LX_OK;
 }
 
 extern "C" LX_API lx_status lx_batch_remove(lx_batch* b, lx_sim* s) {
   if (!b || !s) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  lx_status st = lx_batch_wait(b);
+  if (st) return st;
   for (size_t q = 0; q < b->sims.size(); q++)
     if (b->sims[q] == s) {
-      BCK(cudaStreamSynchronize(b->stream));
       b->sims.erase(b->sims.begin() + q);
+      s->batch = nullptr;
       b->dirty = true;
       if (b->sims.empty()) b->prec = -1;
       return LX_OK;
@@ -1450,16 +1498,14 @@ extern "C" LX_API lx_status lx_batch_remove(lx_batch* b, lx_sim* s) {
 
 template <class T, class C>
 static lx_status batch_rebuild(lx_batch* b) {
-  BCK(cudaStreamSynchronize(b->stream));
   batch_free_device(b);
   const int n = (int)b->sims.size();
   std::vector<lx::PrologueParams> pps(n);
-  std::vector<lx::DftParams> dfts;
   b->max_entries = 0;
-  b->need_prologue = false;
-  b->max_cells4 = 0;
   b->host_ts.resize(n);
+  b->graphable = true;
   BCK(cudaMallocAsync(&b->d_slots, sizeof(unsigned long long) * (n > 0 ? n : 1), b->stream));
+  std::vector<std::vector<lx::DftParams>> dft_planes;
   for (int q = 0; q < n; q++) {
     lx_sim* s = b->sims[q];
     pps[q] = make_prologue(s);
@@ -1472,15 +1518,26 @@ static lx_status batch_rebuild(lx_batch* b) {
       std::memset(&dp, 0, sizeof dp);
       dp.axis = d.axis; dp.index = d.index; dp.na = d.na; dp.nb = d.nb; dp.Ny = s->Ny; dp.Nzp = s->Nzp;
       dp.nfreq = d.nfreq; dp.dt = s->k.dt; dp.weight = (double)d.every; dp.every_ = d.every;
-      dp.omega = d.d_omega; dp.acc = d.d_acc; dp.sim = q;
+      dp.omega = d.d_omega; dp.acc = d.d_acc; dp.sim = q; dp.hmul = 1.0 / s->hscale;
       for (int c = 0; c < 4; c++) {
         dp.f[c] = pf[d.comps[c]];
         for (int a = 0; a < 3; a++) dp.ext[c][a] = s->ext[d.comps[c]][a];
       }
-      dfts.push_back(dp);
-      b->max_cells4 = std::max(b->max_cells4, 4LL * d.na * d.nb);
+      // sampled at batch steps b' with (t + b' - step) % every == 0
+      const int phase = (int)(((b->step - s->t) % d.every + d.every) % d.every);
+      int ci = -1;
+      for (size_t k = 0; k < b->dft.size(); k++)
+        if (b->dft[k].every == d.every && b->dft[k].phase == phase) ci = (int)k;
+      if (ci < 0) {
+        b->dft.emplace_back();
+        b->dft.back().every = d.every;
+        b->dft.back().phase = phase;
+        dft_planes.emplace_back();
+        ci = (int)b->dft.size() - 1;
+      }
+      dft_planes[ci].push_back(dp);
+      if (b->chunk > 0 && b->chunk % d.every != 0) b->graphable = false;
     }
-    // groups by (planar, uniform)
     int gi = -1;
     for (size_t g = 0; g < b->groups.size(); g++)
       if (b->groups[g].planar == (bool)s->planar && b->groups[g].uniform == (bool)s->uniform) gi = (int)g;
@@ -1492,84 +1549,89 @@ static lx_status batch_rebuild(lx_batch* b) {
     }
     b->groups[gi].members.push_back(q);
   }
-  b->need_prologue = n > 0;  // monitor slots are reset every step
   BCK(cudaMallocAsync(&b->d_pps, sizeof(lx::PrologueParams) * (n > 0 ? n : 1), b->stream));
   BCK(cudaMemcpyAsync(b->d_pps, pps.data(), sizeof(lx::PrologueParams) * n, cudaMemcpyHostToDevice, b->stream));
   BCK(cudaMallocAsync(&b->d_ts, sizeof(int) * (n > 0 ? n : 1), b->stream));
   BCK(cudaMemcpyAsync(b->d_ts, b->host_ts.data(), sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
-  b->ndft = (int)dfts.size();
-  if (b->ndft) {
-    BCK(cudaMallocAsync(&b->d_dfts, sizeof(lx::DftParams) * b->ndft, b->stream));
-    BCK(cudaMemcpyAsync(b->d_dfts, dfts.data(), sizeof(lx::DftParams) * b->ndft, cudaMemcpyHostToDevice, b->stream));
+  for (size_t k = 0; k < b->dft.size(); k++) {
+    auto& cl = b->dft[k];
+    const auto& planes = dft_planes[k];
+    std::vector<int> bfirst(planes.size() + 1, 0);
+    for (size_t q = 0; q < planes.size(); q++) bfirst[q + 1] = bfirst[q] + (int)((4LL * planes[q].na * planes[q].nb + 255) / 256);
+    cl.nplanes = (int)planes.size();
+    cl.nblocks = bfirst.back();
+    BCK(cudaMallocAsync(&cl.d_planes, sizeof(lx::DftParams) * planes.size(), b->stream));
+    BCK(cudaMemcpyAsync(cl.d_planes, planes.data(), sizeof(lx::DftParams) * planes.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMallocAsync(&cl.d_bfirst, sizeof(int) * bfirst.size(), b->stream));
+    BCK(cudaMemcpyAsync(cl.d_bfirst, bfirst.data(), sizeof(int) * bfirst.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMallocAsync(&cl.d_map, sizeof(int2) * (cl.nblocks > 0 ? cl.nblocks : 1), b->stream));
+    BCK(lx::launch_block_map(cl.d_bfirst, cl.nplanes, cl.nblocks, cl.d_map, b->stream));
   }
   for (auto& g : b->groups) {
     std::vector<lx::StepParams<T, C>> ps;
-    std::vector<lx::Tile> tiles;
-    for (size_t li = 0; li < g.members.size(); li++) {
-      lx_sim* s = b->sims[g.members[li]];
+    std::vector<int> first(1, 0);
+    for (int q : g.members) {
+      lx_sim* s = b->sims[q];
       lx::StepParams<T, C> sp = step_params<T, C>(s);
-      sp.max_slot = b->d_slots + g.members[li];
+      sp.max_slot = b->d_slots + q;
       sp.etotal = nullptr;
       ps.push_back(sp);
-      if (s->planar) {
-        for (int i0 = 0; i0 < s->Nx; i0 += 8 * lx::kMarch)
-          for (int k0 = 0; k0 < s->Nz; k0 += 32) tiles.push_back({(int)li, i0, 0, k0});
-      } else {
-        for (int i = 0; i < s->Nx; i += lx::kMarch)
-          for (int j0 = 0; j0 < s->Ny; j0 += 8)
-            for (int k0 = 0; k0 < s->Nz; k0 += 32) tiles.push_back({(int)li, i, j0, k0});
-      }
+      const long long nb = (long long)first.back() + lx::batch_blocks(s->Nx, s->Ny, s->Nz, s->planar);
+      if (nb > 0x7fffffffLL) return bfail(b, LX_ERR_INVALID, "batch too large for one launch");
+      first.push_back((int)nb);
     }
-    if ((long long)tiles.size() > 0x7fffffffLL) return bfail(b, LX_ERR_INVALID, "batch too large for one launch");
-    g.ntiles = (int)tiles.size();
+    g.nblocks = first.back();
     BCK(cudaMallocAsync(&g.d_params, sizeof(lx::StepParams<T, C>) * ps.size(), b->stream));
     BCK(cudaMemcpyAsync(g.d_params, ps.data(), sizeof(lx::StepParams<T, C>) * ps.size(), cudaMemcpyHostToDevice, b->stream));
-    BCK(cudaMallocAsync(&g.d_tiles, sizeof(lx::Tile) * (tiles.empty() ? 1 : tiles.size()), b->stream));
-    BCK(cudaMemcpyAsync(g.d_tiles, tiles.data(), sizeof(lx::Tile) * tiles.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMallocAsync(&g.d_first, sizeof(int) * first.size(), b->stream));
+    BCK(cudaMemcpyAsync(g.d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMallocAsync(&g.d_tiles, sizeof(int4) * (g.nblocks > 0 ? g.nblocks : 1), b->stream));
+    BCK(lx::launch_batch_tiles<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_first, (int)g.members.size(), g.nblocks,
+                                     g.planar, g.d_tiles, b->stream));
   }
   b->dirty = false;
   return LX_OK;
 }
 
 template <class T, class C>
-static lx_status batch_enqueue(lx_batch* b, int nsteps) {
+static lx_status batch_enqueue(lx_batch* b, long long step0, int nsteps) {
   const int n = (int)b->sims.size();
   for (int q = 0; q < nsteps; q++) {
-    if (b->need_prologue) BCK(lx::launch_prologue_batch<C>(b->d_pps, b->d_ts, n, b->max_entries, b->stream));
+    BCK(lx::launch_prologue_batch<C>(b->d_pps, b->d_ts, n, b->max_entries, b->stream));
     for (auto& g : b->groups)
-      BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.ntiles, g.planar, g.uniform,
-                                      true, b->stream));
+      BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.nblocks, g.planar,
+                                      g.uniform, true, b->stream));
     for (auto& g : b->groups)
-      BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.ntiles, g.planar, g.uniform,
-                                      false, b->stream));
-    if (b->ndft) BCK(lx::launch_dft_batch<T>(b->d_dfts, b->ndft, b->max_cells4, b->d_ts, b->stream));
+      BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.nblocks, g.planar,
+                                      g.uniform, false, b->stream));
+    const long long bs = step0 + q;
+    for (auto& cl : b->dft)
+      if (bs % cl.every == cl.phase)
+        BCK(lx::launch_dft_batch<T>(cl.d_planes, cl.d_map, cl.nblocks, b->d_ts, b->stream));
     BCK(lx::launch_tick(b->d_ts, n, b->stream));
   }
   return LX_OK;
 }
 
 template <class T, class C>
-static lx_status batch_run(lx_batch* b, int nsteps) {
+static lx_status batch_run_async(lx_batch* b, int nsteps) {
   lx_status st;
-  // a member stepped on its own since the last batch step -> re-read step counters
   bool moved = false;
   for (size_t q = 0; q < b->sims.size() && !b->dirty; q++) moved |= (b->sims[q]->t != b->host_ts[q]);
-  if (b->dirty) {
+  if (b->dirty || moved) {
+    for (auto* s : b->sims) BCK(cudaStreamSynchronize(s->stream));  // members' own pending work first
     if ((st = batch_rebuild<T, C>(b))) return st;
-  } else if (moved) {
-    for (size_t q = 0; q < b->sims.size(); q++) b->host_ts[q] = b->sims[q]->t;
-    BCK(cudaMemcpyAsync(b->d_ts, b->host_ts.data(), sizeof(int) * b->sims.size(), cudaMemcpyHostToDevice, b->stream));
   }
-  for (auto* s : b->sims) BCK(cudaStreamSynchronize(s->stream));  // members' own pending work first
   int done = 0;
-  if (b->chunk > 0) {
+  if (b->chunk > 0 && b->graphable) {
     while (nsteps - done >= b->chunk) {
-      if (!b->exec || b->exec_steps != b->chunk) {
+      const long long base_mod = b->step % b->chunk;
+      if (!b->exec || b->exec_steps != b->chunk || b->exec_base_mod != base_mod) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
         cudaGraph_t g;
         BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        st = batch_enqueue<T, C>(b, b->chunk);
+        st = batch_enqueue<T, C>(b, b->step, b->chunk);
         cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
         if (st) return st;
         BCK(ce);
@@ -1577,27 +1639,47 @@ static lx_status batch_run(lx_batch* b, int nsteps) {
         cudaGraphDestroy(g);
         BCK(ce);
         b->exec_steps = b->chunk;
+        b->exec_base_mod = base_mod;
       }
       BCK(cudaGraphLaunch(b->exec, b->stream));
+      b->step += b->chunk;
       done += b->chunk;
     }
   }
   if (nsteps - done > 0) {
-    if ((st = batch_enqueue<T, C>(b, nsteps - done))) return st;
+    if ((st = batch_enqueue<T, C>(b, b->step, nsteps - done))) return st;
+    b->step += nsteps - done;
   }
+  for (size_t q = 0; q < b->sims.size(); q++) {
+    b->sims[q]->t += nsteps;
+    b->host_ts[q] = b->sims[q]->t;
+    b->sims[q]->n_kernels += (uint64_t)nsteps * 4;
+  }
+  b->pending += nsteps;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_batch_step_async(lx_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return fail(nullptr, LX_ERR_INVALID, "bad argument");
+  if (b->sims.empty() || nsteps == 0) return LX_OK;
+  if (b->prec == LX_PREC_FP64) return batch_run_async<double, double>(b, nsteps);
+  if (b->prec == LX_PREC_FP32) return batch_run_async<float, float>(b, nsteps);
+  return batch_run_async<__half, float>(b, nsteps);
+}
+
+extern "C" LX_API lx_status lx_batch_wait(lx_batch* b) {
+  if (!b) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  if (b->pending == 0) return LX_OK;
   const int n = (int)b->sims.size();
   std::vector<unsigned long long> slots(n);
   if (n) BCK(cudaMemcpyAsync(slots.data(), b->d_slots, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
+  b->pending = 0;
   std::string bad;
   for (int q = 0; q < n; q++) {
-    lx_sim* s = b->sims[q];
-    s->t += nsteps;
-    b->host_ts[q] = s->t;
-    s->n_kernels += (uint64_t)nsteps * 4;
     double v;
     std::memcpy(&v, &slots[q], sizeof v);
-    s->last_max = v;
+    b->sims[q]->last_max = v;
     if (!std::isfinite(v) && bad.empty()) bad = "member " + std::to_string(q) + ": max|E|^2 is not finite";
   }
   if (!bad.empty()) return bfail(b, LX_ERR_BLOWUP, bad);
@@ -1605,9 +1687,7 @@ static lx_status batch_run(lx_batch* b, int nsteps) {
 }
 
 extern "C" LX_API lx_status lx_batch_step(lx_batch* b, int nsteps) {
-  if (!b || nsteps < 0) return fail(nullptr, LX_ERR_INVALID, "bad argument");
-  if (b->sims.empty() || nsteps == 0) return LX_OK;
-  if (b->prec == LX_PREC_FP64) return batch_run<double, double>(b, nsteps);
-  if (b->prec == LX_PREC_FP32) return batch_run<float, float>(b, nsteps);
-  return batch_run<__half, float>(b, nsteps);
+  lx_status st = lx_batch_step_async(b, nsteps);
+  if (st) return st;
+  return lx_batch_wait(b);
 }

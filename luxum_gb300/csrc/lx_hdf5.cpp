@@ -22,7 +22,7 @@
 #include <cstring>
 #include <sstream>
 
-#include "../../include/luxum.h"
+#include "luxum.h"
 
 namespace lx {
 

@@ -58,6 +58,7 @@ struct PatchSet {
   double neg;        // 1, or -1 for the planar H-curl lines that multiply by (-1) first
   double dn;         // spacing along `axis` (the reference divides by it)
   int hcurl;         // 1: also divide by c and mu0 (H-curl lines)
+  double scale;      // stored-H scale for H-curl lines (1 unless H is stored scaled)
 };
 
 // Parameters of the step prologue: TF/SF tables, point source, monitor reset.
@@ -116,17 +117,9 @@ struct StepParams {
 // Probe sampling of one step row.
 struct ProbeParams {
   int nprobes, row, Ny, Nzp;
+  double hmul;      // 1/hscale: stored H -> H
   int ext[6][3];    // staggered extents of the six components (0 for absent ones)
   const int* ijk;   // device array [nprobes][3]
-};
-
-// One tile of a batched launch: 32 (z) x 8 (y) x kMarch (x) cells of one 3-D simulation, or
-// 32 (z) x 8*kMarch (x) cells of a planar one.
-struct Tile {
-  int sim;  // index into the batch's parameter array
-  int a;    // 3-D: first x plane; planar: first x index
-  int b;    // 3-D: first y index
-  int c;    // first z index
 };
 
 // One DFT plane monitor (see lx_sim_add_dft_plane).
@@ -136,6 +129,7 @@ struct DftParams {
   const void* f[4];       // batched launches: the four sampled components
   int ext[4][3];          // extents of the four sampled components
   double dt, weight;
+  double hmul;            // 1/hscale for the two H components
   int every_;             // batched launches: sampling cadence
   const double* omega;    // device [nfreq]
   double* acc;            // device [nfreq][4][na*nb][2]

@@ -16,6 +16,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "lx_internal.h"
 #include "lx_kernels.h"
 
@@ -126,6 +128,7 @@ __device__ double incident_value(const PrologueParams& p, const PatchSet& ps, in
   v = __ddiv_rn(v, ps.dn);
   if (ps.hcurl) v = __ddiv_rn(__ddiv_rn(v, p.c), p.mu0);
   if (p.scale_units == 0.0) v = __dmul_rn(v, ps.dn);  // difference units
+  if (ps.scale != 1.0) v = __dmul_rn(v, ps.scale);   // scaled H storage
   return ps.sign[plane] < 0 ? -v : v;
 }
 
@@ -501,25 +504,64 @@ __global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
 
 // ------------------------------------------------------------------ batched update kernels
 
-// One block per tile of one simulation of the batch; the parameters come from global memory.
+__device__ __forceinline__ int find_member(const int* __restrict__ first, int n, int t) {
+  int lo = 0, hi = n;  // first[lo] <= t < first[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (first[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Block map of a batched launch: member m owns blocks [first[m], first[m+1]).  Built on the
+// device once per change of membership, so that a block of the update kernels finds its
+// member and tile with one 16-byte load: {member, a, b, c} with a = first x plane (3-D) or
+// first x row (planar), b = first y row (3-D), c = first z cell.
+template <class T, class C>
+__global__ void batch_tiles_kernel(const StepParams<T, C>* __restrict__ ps, const int* __restrict__ first, int n,
+                                   int nblocks, int planar, int4* __restrict__ tiles) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nblocks; t += gridDim.x * blockDim.x) {
+    const int m = find_member(first, n, t);
+    const int lt = t - first[m];
+    const StepParams<T, C>& p = ps[m];
+    const int nkb = (p.Nz + 31) / 32;
+    if (planar) {
+      tiles[t] = make_int4(m, (lt / nkb) * 8 * kMarch, 0, (lt % nkb) * 32);
+    } else {
+      const int njb = (p.Ny + 7) / 8;
+      tiles[t] = make_int4(m, (lt / (nkb * njb)) * kMarch, ((lt / nkb) % njb) * 8, (lt % nkb) * 32);
+    }
+  }
+}
+
+// DFT planes of a batch: block -> {plane, block within the plane}.
+__global__ void block_map_kernel(const int* __restrict__ first, int n, int nblocks, int2* __restrict__ map) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nblocks; t += gridDim.x * blockDim.x) {
+    const int m = find_member(first, n, t);
+    map[t] = make_int2(m, t - first[m]);
+  }
+}
+
+// 3-D members: a block is 32 z x 8 y cells over kMarch consecutive x planes.
 template <class T, class C, bool UNI>
-__global__ void __launch_bounds__(256) h_batch_3d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
-  const Tile tl = tiles[blockIdx.x];
-  const StepParams<T, C>& p = ps[tl.sim];
-  const int k = tl.c + threadIdx.x, j = tl.b + threadIdx.y, i0 = tl.a;
+__global__ void __launch_bounds__(256) h_batch_3d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
+  const int4 tl = tiles[blockIdx.x];
+  const StepParams<T, C>& p = ps[tl.x];
+  const int k = tl.w + threadIdx.x, j = tl.z + threadIdx.y, i0 = tl.y;
   if (k >= p.Nz || j >= p.Ny) return;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, kMarch, tl.b, 8, tl.c, 32);
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, kMarch, tl.z, 8, tl.w, 32);
   const int i1 = min(i0 + kMarch, p.Nx);
 #pragma unroll 1
   for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI>(p, i, j, k, tf);
 }
 
 template <class T, class C, bool UNI>
-__global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
-  const Tile tl = tiles[blockIdx.x];
-  const StepParams<T, C>& p = ps[tl.sim];
-  const int k = tl.c + threadIdx.x, j = tl.b + threadIdx.y, i0 = tl.a;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, kMarch, tl.b, 8, tl.c, 32);
+__global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
+  const int4 tl = tiles[blockIdx.x];
+  const StepParams<T, C>& p = ps[tl.x];
+  const int k = tl.w + threadIdx.x, j = tl.z + threadIdx.y, i0 = tl.y;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, kMarch, tl.z, 8, tl.w, 32);
   unsigned long long mbits = 0ull;
   if (k < p.Nz && j < p.Ny) {
     const int i1 = min(i0 + kMarch, p.Nx);
@@ -532,31 +574,32 @@ __global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __rest
   if (p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
+// planar members: a block is 32 z cells x 8*kMarch x rows
 template <class T, class C, bool UNI>
-__global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
-  const Tile tl = tiles[blockIdx.x];
-  const StepParams<T, C>& p = ps[tl.sim];
-  const int k = tl.c + threadIdx.x;
+__global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
+  const int4 tl = tiles[blockIdx.x];
+  const StepParams<T, C>& p = ps[tl.x];
+  const int k = tl.w + threadIdx.x;
   if (k >= p.Nz) return;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesH, tl.a, 8 * kMarch, 0, 1, tl.c, 32);
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, tl.y, 8 * kMarch, 0, 1, tl.w, 32);
 #pragma unroll 1
   for (int r = 0; r < kMarch; ++r) {
-    const int i = tl.a + threadIdx.y + 8 * r;
+    const int i = tl.y + threadIdx.y + 8 * r;
     if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
   }
 }
 
 template <class T, class C, bool UNI>
-__global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const Tile* __restrict__ tiles) {
-  const Tile tl = tiles[blockIdx.x];
-  const StepParams<T, C>& p = ps[tl.sim];
-  const int k = tl.c + threadIdx.x;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesE, tl.a, 8 * kMarch, 0, 1, tl.c, 32);
+__global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
+  const int4 tl = tiles[blockIdx.x];
+  const StepParams<T, C>& p = ps[tl.x];
+  const int k = tl.w + threadIdx.x;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, tl.y, 8 * kMarch, 0, 1, tl.w, 32);
   unsigned long long mbits = 0ull;
   if (k < p.Nz) {
 #pragma unroll 1
     for (int r = 0; r < kMarch; ++r) {
-      const int i = tl.a + threadIdx.y + 8 * r;
+      const int i = tl.y + threadIdx.y + 8 * r;
       if (i < p.Nx) {
         const unsigned long long b = e_cell_2d<T, C, UNI, true>(p, i, k, tf);
         mbits = b > mbits ? b : mbits;
@@ -571,26 +614,27 @@ __global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __rest
 // padded (Nx,Ny,Nzp) storage -> dense double array of extent (n0,n1,n2)
 template <class T>
 __global__ void gather_kernel(const T* __restrict__ src, double* __restrict__ dst, int n0, int n1, int n2, int Ny,
-                              int Nzp) {
+                              int Nzp, double mul) {
   const long long total = (long long)n0 * n1 * n2;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(q % n2);
     const long long r = q / n2;
     const int j = (int)(r % n1);
     const int i = (int)(r / n1);
-    dst[q] = (double)src[((long long)i * Ny + j) * Nzp + k];
+    const double v = (double)src[((long long)i * Ny + j) * Nzp + k];
+    dst[q] = mul == 1.0 ? v : v * mul;
   }
 }
 template <>
 __global__ void gather_kernel<__half>(const __half* __restrict__ src, double* __restrict__ dst, int n0, int n1, int n2,
-                                      int Ny, int Nzp) {
+                                      int Ny, int Nzp, double mul) {
   const long long total = (long long)n0 * n1 * n2;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(q % n2);
     const long long r = q / n2;
     const int j = (int)(r % n1);
     const int i = (int)(r / n1);
-    dst[q] = (double)__half2float(src[((long long)i * Ny + j) * Nzp + k]);
+    dst[q] = (double)__half2float(src[((long long)i * Ny + j) * Nzp + k]) * mul;
   }
 }
 
@@ -649,6 +693,7 @@ __global__ void probe_kernel(const ProbeParams pp, const T* f0, const T* f1, con
     const T* src = f[comp] + ((long long)i * pp.Ny + j) * pp.Nzp + k;
     if constexpr (sizeof(T) == 2) v = (double)__half2float(*src);
     else v = (double)*src;
+    if (comp >= 3 && pp.hmul != 1.0) v *= pp.hmul;
   }
   out[(long long)pp.row * pp.nprobes * 6 + q] = v;
 }
@@ -658,7 +703,7 @@ __global__ void probe_kernel(const ProbeParams pp, const T* f0, const T* f1, con
 // (component, cell) and updates its nfreq complex accumulators (coalesced along the cell).
 template <class T>
 __device__ __forceinline__ void dft_body(const DftParams& d, const int t, const T* f0, const T* f1, const T* f2,
-                                         const T* f3) {
+                                         const T* f3, const int lb) {
   __shared__ double cs[2][kMaxDftFreq], sn[2][kMaxDftFreq];
   for (int f = threadIdx.x; f < d.nfreq; f += blockDim.x) {
     const double pe = __dmul_rn(d.omega[f], __dmul_rn((double)(t + 1), d.dt));
@@ -668,7 +713,7 @@ __device__ __forceinline__ void dft_body(const DftParams& d, const int t, const 
   }
   __syncthreads();
   const long long ncell = (long long)d.na * d.nb;
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long q = lb * (long long)blockDim.x + threadIdx.x;
   if (q >= 4 * ncell) return;
   const int comp = (int)(q / ncell);
   const long long cell = q % ncell;
@@ -684,6 +729,7 @@ __device__ __forceinline__ void dft_body(const DftParams& d, const int t, const 
     if constexpr (sizeof(T) == 2) v = (double)__half2float(*src);
     else v = (double)*src;
   }
+  if (comp >= 2 && d.hmul != 1.0) v = __dmul_rn(v, d.hmul);
   v = __dmul_rn(v, d.weight);
   const int w = comp < 2 ? 0 : 1;
   double2* acc = reinterpret_cast<double2*>(d.acc);
@@ -697,18 +743,49 @@ __device__ __forceinline__ void dft_body(const DftParams& d, const int t, const 
 
 template <class T>
 __global__ void dft_kernel(const DftParams d, const T* f0, const T* f1, const T* f2, const T* f3) {
-  dft_body<T>(d, d.t, f0, f1, f2, f3);
+  dft_body<T>(d, d.t, f0, f1, f2, f3, blockIdx.x);
 }
 
-// Batched DFT planes: blockIdx.y selects the plane; sampled when the owner's step counter
-// (before this step's tick) is a multiple of the plane's cadence.
+// Batched DFT planes: a flat launch over the planes sampled at this step; bfirst[q] is the
+// first block of plane q (each block serves one plane, so its phase table is per plane).
 template <class T>
-__global__ void dft_batch_kernel(const DftParams* __restrict__ ds, const int* __restrict__ ts) {
-  const DftParams& d = ds[blockIdx.y];
+__global__ void dft_batch_kernel(const DftParams* __restrict__ ds, const int2* __restrict__ map, const int* __restrict__ ts) {
+  const int2 bm = map[blockIdx.x];
+  const DftParams& d = ds[bm.x];
   const int t = ts[d.sim];
   if (t % d.every_ != 0) return;
-  if ((long long)blockIdx.x * blockDim.x >= 4LL * d.na * d.nb) return;
-  dft_body<T>(d, t, (const T*)d.f[0], (const T*)d.f[1], (const T*)d.f[2], (const T*)d.f[3]);
+  dft_body<T>(d, t, (const T*)d.f[0], (const T*)d.f[1], (const T*)d.f[2], (const T*)d.f[3], bm.y);
+}
+
+// Net flux of a DFT plane per frequency: partial sums over fixed chunks of 1024 cells, then
+// the chunks summed in order, so the result does not depend on scheduling.
+__global__ void dft_flux_partial(const double* __restrict__ acc, int nfreq, long long ncell, double* __restrict__ part,
+                                 int nchunk) {
+  const int f = blockIdx.y, ch = blockIdx.x;
+  const double2* a = reinterpret_cast<const double2*>(acc);
+  double v = 0.0;
+  const long long c0 = (long long)ch * 1024;
+  for (long long c = c0 + threadIdx.x; c < c0 + 1024 && c < ncell; c += blockDim.x) {
+    const double2 e1 = a[((long long)f * 4 + 0) * ncell + c], e2 = a[((long long)f * 4 + 1) * ncell + c];
+    const double2 h1 = a[((long long)f * 4 + 2) * ncell + c], h2 = a[((long long)f * 4 + 3) * ncell + c];
+    v += (e1.x * h2.x + e1.y * h2.y) - (e2.x * h1.x + e2.y * h1.y);
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[(long long)f * nchunk + ch] = red[0];
+}
+
+__global__ void dft_flux_final(const double* __restrict__ part, int nfreq, int nchunk, double dA, double* __restrict__ out) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nfreq) return;
+  double v = 0.0;
+  for (int c = 0; c < nchunk; ++c) v += part[(long long)f * nchunk + c];
+  out[f] = v * dA;
 }
 
 // ------------------------------------------------------------------ launchers
@@ -762,10 +839,10 @@ cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bo
 }
 
 template <class T>
-cudaError_t launch_gather(const T* src, double* dst, const int ext[3], int Ny, int Nzp, cudaStream_t s) {
+cudaError_t launch_gather(const T* src, double* dst, const int ext[3], int Ny, int Nzp, double mul, cudaStream_t s) {
   const long long n = (long long)ext[0] * ext[1] * ext[2];
   if (n == 0) return cudaSuccess;
-  gather_kernel<T><<<grid1d(n, 256), 256, 0, s>>>(src, dst, ext[0], ext[1], ext[2], Ny, Nzp);
+  gather_kernel<T><<<grid1d(n, 256), 256, 0, s>>>(src, dst, ext[0], ext[1], ext[2], Ny, Nzp, mul);
   return cudaGetLastError();
 }
 
@@ -801,27 +878,46 @@ cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s) {
 }
 
 template <class T, class C>
-cudaError_t launch_batch_step(const StepParams<T, C>* ps, const Tile* tiles, int ntiles, bool planar, bool uniform,
+cudaError_t launch_batch_tiles(const StepParams<T, C>* ps, const int* first, int n, int nblocks, bool planar, int4* tiles,
+                               cudaStream_t s) {
+  if (nblocks <= 0) return cudaSuccess;
+  batch_tiles_kernel<T, C><<<grid1d(nblocks, 256), 256, 0, s>>>(ps, first, n, nblocks, planar ? 1 : 0, tiles);
+  return cudaGetLastError();
+}
+
+template <class T, class C>
+cudaError_t launch_batch_step(const StepParams<T, C>* ps, const int4* tiles, int nblocks, bool planar, bool uniform,
                               bool h_half, cudaStream_t s) {
-  if (ntiles <= 0) return cudaSuccess;
+  if (nblocks <= 0) return cudaSuccess;
   dim3 block(32, 8);
   if (planar) {
     if (h_half) {
-      if (uniform) h_batch_2d<T, C, true><<<ntiles, block, 0, s>>>(ps, tiles);
-      else h_batch_2d<T, C, false><<<ntiles, block, 0, s>>>(ps, tiles);
+      if (uniform) h_batch_2d<T, C, true><<<nblocks, block, 0, s>>>(ps, tiles);
+      else h_batch_2d<T, C, false><<<nblocks, block, 0, s>>>(ps, tiles);
     } else {
-      if (uniform) e_batch_2d<T, C, true><<<ntiles, block, 0, s>>>(ps, tiles);
-      else e_batch_2d<T, C, false><<<ntiles, block, 0, s>>>(ps, tiles);
+      if (uniform) e_batch_2d<T, C, true><<<nblocks, block, 0, s>>>(ps, tiles);
+      else e_batch_2d<T, C, false><<<nblocks, block, 0, s>>>(ps, tiles);
     }
   } else {
     if (h_half) {
-      if (uniform) h_batch_3d<T, C, true><<<ntiles, block, 0, s>>>(ps, tiles);
-      else h_batch_3d<T, C, false><<<ntiles, block, 0, s>>>(ps, tiles);
+      if (uniform) h_batch_3d<T, C, true><<<nblocks, block, 0, s>>>(ps, tiles);
+      else h_batch_3d<T, C, false><<<nblocks, block, 0, s>>>(ps, tiles);
     } else {
-      if (uniform) e_batch_3d<T, C, true><<<ntiles, block, 0, s>>>(ps, tiles);
-      else e_batch_3d<T, C, false><<<ntiles, block, 0, s>>>(ps, tiles);
+      if (uniform) e_batch_3d<T, C, true><<<nblocks, block, 0, s>>>(ps, tiles);
+      else e_batch_3d<T, C, false><<<nblocks, block, 0, s>>>(ps, tiles);
     }
   }
+  return cudaGetLastError();
+}
+
+int batch_blocks(int Nx, int Ny, int Nz, bool planar) {
+  if (planar) return ((Nz + 31) / 32) * ((Nx + 8 * kMarch - 1) / (8 * kMarch));
+  return ((Nz + 31) / 32) * ((Ny + 7) / 8) * ((Nx + kMarch - 1) / kMarch);
+}
+
+cudaError_t launch_block_map(const int* first, int n, int nblocks, int2* map, cudaStream_t s) {
+  if (nblocks <= 0) return cudaSuccess;
+  block_map_kernel<<<grid1d(nblocks, 256), 256, 0, s>>>(first, n, nblocks, map);
   return cudaGetLastError();
 }
 
@@ -842,22 +938,32 @@ cudaError_t launch_tick(int* ts, int n, cudaStream_t s) {
 }
 
 template <class T>
-cudaError_t launch_dft_batch(const DftParams* ds, int nplanes, long long max_cells4, const int* ts, cudaStream_t s) {
-  if (nplanes <= 0) return cudaSuccess;
-  dft_batch_kernel<T><<<dim3((unsigned)((max_cells4 + 255) / 256), (unsigned)nplanes), 256, 0, s>>>(ds, ts);
+cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nblocks, const int* ts, cudaStream_t s) {
+  if (nblocks <= 0) return cudaSuccess;
+  dft_batch_kernel<T><<<nblocks, 256, 0, s>>>(ds, map, ts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dft_flux(const double* acc, int nfreq, long long ncell, double* part, double dA, double* out,
+                            cudaStream_t s) {
+  const int nchunk = (int)((ncell + 1023) / 1024);
+  dft_flux_partial<<<dim3(nchunk, nfreq), 256, 0, s>>>(acc, nfreq, ncell, part, nchunk);
+  dft_flux_final<<<(nfreq + 63) / 64, 64, 0, s>>>(part, nfreq, nchunk, dA, out);
   return cudaGetLastError();
 }
 
 #define LX_INST(T, C)                                                                                                  \
   template cudaError_t launch_step<T, C>(const StepParams<T, C>&, bool, bool, bool, cudaStream_t);                   \
-  template cudaError_t launch_gather<T>(const T*, double*, const int[3], int, int, cudaStream_t);                     \
+  template cudaError_t launch_gather<T>(const T*, double*, const int[3], int, int, double, cudaStream_t);                     \
   template cudaError_t launch_scatter<T>(const double*, T*, const int[3], int, int, int, double, double, double,      \
                                          double, cudaStream_t);                                                        \
   template cudaError_t launch_probes<T>(const ProbeParams&, T* const[6], double*, cudaStream_t);                   \
   template cudaError_t launch_dft<T>(const DftParams&, T* const[4], cudaStream_t);                                 \
-  template cudaError_t launch_batch_step<T, C>(const StepParams<T, C>*, const Tile*, int, bool, bool, bool,         \
+  template cudaError_t launch_batch_tiles<T, C>(const StepParams<T, C>*, const int*, int, int, bool, int4*,         \
+                                                cudaStream_t);                                                     \
+  template cudaError_t launch_batch_step<T, C>(const StepParams<T, C>*, const int4*, int, bool, bool, bool,     \
                                                cudaStream_t);                                                          \
-  template cudaError_t launch_dft_batch<T>(const DftParams*, int, long long, const int*, cudaStream_t);
+  template cudaError_t launch_dft_batch<T>(const DftParams*, const int2*, int, const int*, cudaStream_t);
 LX_INST(double, double)
 LX_INST(float, float)
 LX_INST(__half, float)

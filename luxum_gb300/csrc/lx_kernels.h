@@ -11,7 +11,7 @@ cudaError_t launch_prologue(const PrologueParams& p, cudaStream_t s);
 template <class T, class C>
 cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bool h_half, cudaStream_t s);
 template <class T>
-cudaError_t launch_gather(const T* src, double* dst, const int ext[3], int Ny, int Nzp, cudaStream_t s);
+cudaError_t launch_gather(const T* src, double* dst, const int ext[3], int Ny, int Nzp, double mul, cudaStream_t s);
 template <class T>
 cudaError_t launch_scatter(const double* src, T* dst, const int ext[3], int Ny, int Nzp, int mode, double a, double dt,
                            double eps0, double scale, cudaStream_t s);
@@ -24,13 +24,24 @@ cudaError_t launch_probes(const ProbeParams& pp, T* const f[6], double* out, cud
 template <class T>
 cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s);
 
+// Batched updates: member m of a group owns blocks [first[m], first[m+1]) of each launch;
+// launch_batch_tiles turns that prefix into the per-block tile map the update kernels read.
 template <class T, class C>
-cudaError_t launch_batch_step(const StepParams<T, C>* ps, const Tile* tiles, int ntiles, bool planar, bool uniform,
+cudaError_t launch_batch_tiles(const StepParams<T, C>* ps, const int* first, int n, int nblocks, bool planar, int4* tiles,
+                               cudaStream_t s);
+template <class T, class C>
+cudaError_t launch_batch_step(const StepParams<T, C>* ps, const int4* tiles, int nblocks, bool planar, bool uniform,
                               bool h_half, cudaStream_t s);
+// blocks one member occupies in a batched update launch
+int batch_blocks(int Nx, int Ny, int Nz, bool planar);
+// block -> {member, block within the member} for a prefix `first` of n members
+cudaError_t launch_block_map(const int* first, int n, int nblocks, int2* map, cudaStream_t s);
 template <class C>
 cudaError_t launch_prologue_batch(const PrologueParams* pps, const int* ts, int nsims, int max_entries, cudaStream_t s);
 cudaError_t launch_tick(int* ts, int n, cudaStream_t s);
 template <class T>
-cudaError_t launch_dft_batch(const DftParams* ds, int nplanes, long long max_cells4, const int* ts, cudaStream_t s);
+cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nblocks, const int* ts, cudaStream_t s);
+cudaError_t launch_dft_flux(const double* acc, int nfreq, long long ncell, double* part, double dA, double* out,
+                            cudaStream_t s);
 
 }  // namespace lx

@@ -26,7 +26,7 @@
 #include <mutex>
 #include <string>
 
-#include "../../include/luxum.h"
+#include "luxum.h"
 #include "lx_sim.h"
 
 namespace lx {
@@ -63,7 +63,7 @@ cudaError_t staging_address(double** out) {
 // padded (Nx,Ny,Nzp) storage -> dense doubles of extent (n0,n1,n2) in the static array
 template <class T>
 __global__ void gather_to_staging(const T* __restrict__ src, double* __restrict__ dst, int n0, int n1, int n2, int Ny,
-                                  int Nzp) {
+                                  int Nzp, double mul) {
   const long long total = (long long)n0 * n1 * n2;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(q % n2);
@@ -71,17 +71,19 @@ __global__ void gather_to_staging(const T* __restrict__ src, double* __restrict_
     const int j = (int)(r % n1);
     const int i = (int)(r / n1);
     const T v = src[((long long)i * Ny + j) * Nzp + k];
-    if constexpr (sizeof(T) == 2) dst[q] = (double)__half2float(v);
-    else dst[q] = (double)v;
+    double w;
+    if constexpr (sizeof(T) == 2) w = (double)__half2float(v);
+    else w = (double)v;
+    dst[q] = mul == 1.0 ? w : w * mul;  // H stored scaled (FP16 storage)
   }
 }
 
 template <class T>
-void launch(const void* src, double* dst, const int ext[3], int Ny, int Nzp, cudaStream_t s) {
+void launch(const void* src, double* dst, const int ext[3], int Ny, int Nzp, double mul, cudaStream_t s) {
   const long long n = (long long)ext[0] * ext[1] * ext[2];
   long long g = (n + 255) / 256;
   if (g > 152LL * 64) g = 152LL * 64;
-  gather_to_staging<T><<<(unsigned)(g < 1 ? 1 : g), 256, 0, s>>>((const T*)src, dst, ext[0], ext[1], ext[2], Ny, Nzp);
+  gather_to_staging<T><<<(unsigned)(g < 1 ? 1 : g), 256, 0, s>>>((const T*)src, dst, ext[0], ext[1], ext[2], Ny, Nzp, mul);
 }
 
 }  // namespace
@@ -99,15 +101,20 @@ extern "C" LX_API lx_status lx_sim_read_field_noalloc(lx_sim* s, int comp, doubl
     return bad(LX_ERR_INVALID, "component has " + std::to_string(m) + " values; lx_sim_read_field_noalloc handles at most " +
                                    std::to_string(kLxNoAllocMaxElems) + " (8 MiB of static staging); use lx_sim_read_field");
   if (m == 0) return LX_OK;
+  if (s->batch) {  // a batch chunk in flight writes this handle's fields
+    const lx_status st = lx_batch_wait(s->batch);
+    if (st && st != LX_ERR_BLOWUP) return st;
+  }
   const void* src = comp <= LX_EZ ? s->E[comp] : (comp <= LX_HZ ? s->H[comp - 3] : s->etotal);
   if (!src) return bad(LX_ERR_STATE, comp == LX_ETOTAL ? "|E|^2 is only kept when a snapshot asks for it" : "component absent");
   double* staging = nullptr;
   cudaError_t e = staging_address(&staging);
   if (e != cudaSuccess) return bad(LX_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
   const bool compute_prec = comp == LX_ETOTAL;
-  if ((compute_prec ? s->csize == 8 : s->prec == LX_PREC_FP64)) launch<double>(src, staging, s->ext[comp], s->Ny, s->Nzp, s->stream);
-  else if (compute_prec || s->prec == LX_PREC_FP32) launch<float>(src, staging, s->ext[comp], s->Ny, s->Nzp, s->stream);
-  else launch<__half>(src, staging, s->ext[comp], s->Ny, s->Nzp, s->stream);
+  const double mul = (comp >= LX_HX && comp <= LX_HZ) ? 1.0 / s->hscale : 1.0;
+  if ((compute_prec ? s->csize == 8 : s->prec == LX_PREC_FP64)) launch<double>(src, staging, s->ext[comp], s->Ny, s->Nzp, mul, s->stream);
+  else if (compute_prec || s->prec == LX_PREC_FP32) launch<float>(src, staging, s->ext[comp], s->Ny, s->Nzp, mul, s->stream);
+  else launch<__half>(src, staging, s->ext[comp], s->Ny, s->Nzp, mul, s->stream);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(host, staging, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);

@@ -9,7 +9,7 @@
 #include <thread>
 #include <vector>
 
-#include "../../include/luxum.h"
+#include "luxum.h"
 #include "lx_internal.h"
 
 namespace lx {
@@ -41,6 +41,7 @@ struct DftPlane {
   std::vector<double> omega;
   double* d_omega = nullptr;
   double* d_acc = nullptr;
+  double* d_flux = nullptr;  // flux result + per-chunk partial sums
   size_t n_acc = 0;  // doubles
 };
 
@@ -63,6 +64,7 @@ struct Consts {
 
 struct lx_sim {
   lx_params p;
+  lx_batch* batch = nullptr;  // the batch this handle is a member of
   lx::Consts k;
   std::string err;
   int planar = 0, pml = 0, uniform = 0, prec = 0, tfsf = 0;
@@ -87,7 +89,8 @@ struct lx_sim {
   void* etotal = nullptr;
   double* xfer = nullptr;  // compact staging for field/material transfers
   size_t xfer_cap = 0;
-  double cbs_scale = 1.0;  // 1/dx in difference units, 1 otherwise
+  double cbs_scale = 1.0;  // 1/dx in difference units, 1 otherwise, divided by hscale
+  double hscale = 1.0;     // H is stored as H*hscale (FP16 storage: the impedance of free space)
   double cb0 = 0.0;        // dt/epsilon0
   // point source
   int src_kind = -1;

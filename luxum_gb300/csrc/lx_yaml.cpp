@@ -16,7 +16,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/luxum.h"
+#include "luxum.h"
 
 namespace lx {
 lx_status set_thread_error(const char* msg, lx_status st);

@@ -65,6 +65,16 @@ class Sim:
         self.h = h
         self._cb = None
 
+    @classmethod
+    def _adopt(cls, h: C.c_void_p, p: Params) -> "Sim":
+        """Wraps a handle created elsewhere (a finished server request)."""
+        self = cls.__new__(cls)
+        self.lib = _ffi.lib()
+        self.p = p
+        self.h = h
+        self._cb = None
+        return self
+
     # -- lifecycle
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -273,6 +283,12 @@ class Batch:
 
     def step(self, n: int) -> None:
         self._check(self.lib.lx_batch_step(self.h, n))
+
+    def step_async(self, n: int) -> None:
+        self._check(self.lib.lx_batch_step_async(self.h, n))
+
+    def wait(self) -> None:
+        self._check(self.lib.lx_batch_wait(self.h))
 
     def __len__(self):
         return self.lib.lx_batch_size(self.h)

@@ -92,3 +92,28 @@ def test_device_bytes_estimate(engine, name):
     held = s.info()["device_bytes"]
     assert 0.9 * held <= est <= 1.1 * held + 4096, (est, held)
     s.close()
+
+
+def test_batch_async_equals_blocking(engine):
+    """lx_batch_step_async + lx_batch_wait give what lx_batch_step gives, and host work
+    between the two (creating a handle, stepping it alone) does not disturb the chunk."""
+    from luxum_gb300 import Batch
+
+    a = [_make(n, 1) for n in NAMES]
+    b = [_make(n, 1) for n in NAMES]
+    ba, bb = Batch(chunk=10), Batch(chunk=10)
+    for m in a:
+        ba.add(m)
+    for m in b:
+        bb.add(m)
+    for _ in range(3):
+        ba.step_async(20)
+        extra = _make("planar_oblique", 1)
+        extra.step(3)
+        extra.close()
+        ba.wait()
+        bb.step(20)
+    for m, t in zip(a, b):
+        _same(m, t)
+    ba.close()
+    bb.close()

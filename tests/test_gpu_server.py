@@ -1,0 +1,124 @@
+"""Serving (lx_server_*): continuous batching must not change any request's result.
+
+Requests with different grids, step counts and arrival times share chunks; each must end
+exactly where a handle stepped alone ends (fields, DFT flux, max|E|^2 bit for bit), while
+the worker admits under the budget, cancels on request and fails only the request that
+blows up.
+"""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+W = 2 * np.pi * np.linspace(3e10, 1.5e11, 6)
+REQS = [  # (case, steps, boxes, dft)
+    ("planar_pml_axis", 137, [((20, 0, 20), (30, 1, 40), 4.0)], (0, 45, W, 1)),
+    ("3d_pml_axis", 64, [((12, 10, 12), (18, 16, 20), 6.0)], (0, 20, W, 2)),
+    ("planar_oblique", 250, [], (2, 28, W, 5)),
+    ("3d_oblique", 40, [((10, 10, 10), (14, 20, 16), 2.5)], None),
+]
+
+
+def _params(name):
+    p, _, _ = cases.build(name)
+    p.precision = 1
+    return p
+
+
+def _solo(name, steps, boxes, dft):
+    from luxum_gb300 import Sim
+
+    s = Sim(_params(name))
+    for lo, hi, eps in boxes:
+        s.set_eps_box(lo, hi, eps)
+    plane = None
+    if dft is not None:
+        axis, index, w, every = dft
+        plane = s.add_dft_plane(axis, index, w, every=every)
+    s.step(steps)
+    return s, plane
+
+
+def test_server_results_equal_solo(engine):
+    from luxum_gb300 import Server
+
+    with Server(chunk=50) as srv:
+        ids = [srv.submit(_params(n), steps, boxes, dft) for n, steps, boxes, dft in REQS]
+        for rid in ids:
+            assert srv.wait(rid, 120.0) == "done", srv.error(rid)
+        for rid, (n, steps, boxes, dft) in zip(ids, REQS):
+            twin, plane = _solo(n, steps, boxes, dft)
+            if dft is not None:
+                assert np.array_equal(srv.flux(rid), twin.dft_flux(plane))
+            assert srv.max_e2(rid) == twin.max_e2()
+            t = srv.times(rid)
+            assert 0 <= t[0] <= t[1] <= t[2]
+            g = srv.take(rid, _params(n))
+            assert g.t == steps
+            for c in range(6):
+                if np.prod(g.shape(c)):
+                    assert np.array_equal(g.field(c), twin.field(c)), (n, c)
+            g.close()
+            twin.close()
+        st = srv.stats()
+        assert st["done"] == len(REQS) and st["running"] == 0 and st["queued"] == 0
+        assert st["cell_updates"] > 0 and st["bytes_running"] == pytest.approx(0.0, abs=1.0)
+
+
+def test_server_budget_and_cancel(engine):
+    from luxum_gb300 import Server, device_bytes
+
+    p = _params("planar_oblique")
+    # room for one request at a time
+    with Server(chunk=20, budget_bytes=1.5 * device_bytes(p)) as srv:
+        a = srv.submit(p, 400)
+        b = srv.submit(p, 400)
+        c = srv.submit(p, 60)
+        srv.cancel(b)  # still queued behind a
+        assert srv.wait(b, 10.0) == "cancelled"
+        assert srv.wait(c, 120.0) == "done"
+        st = srv.stats()
+        assert st["peak_running"] == 1
+        assert st["cancelled"] == 1 and st["done"] == 2
+        assert srv.times(a)[2] <= srv.times(c)[1]  # c started after a finished
+        for rid in (a, b, c):
+            srv.release(rid)
+        # a running request leaves at the next chunk end
+        d = srv.submit(p, 100000)
+        while srv.state(d) != "running":
+            srv.wait(d, 0.05)
+        srv.cancel(d)
+        assert srv.wait(d, 60.0) == "cancelled"
+
+
+def test_server_fails_only_the_blown_up_request(engine):
+    from luxum_gb300 import Server
+
+    good = _params("planar_oblique")
+    bad = _params("planar_oblique")
+    bad.S = 3.0  # far past the Courant limit: FP32 overflows within ~50 steps
+    with Server(chunk=25) as srv:
+        rb = srv.submit(bad, 300)
+        rg = srv.submit(good, 300)
+        assert srv.wait(rb, 120.0) == "failed"
+        assert "not finite" in srv.error(rb)
+        assert srv.wait(rg, 120.0) == "done"
+        twin, _ = _solo("planar_oblique", 300, [], None)
+        g = srv.take(rg, good)
+        assert np.array_equal(g.field(1), twin.field(1))
+
+
+def test_server_rejects_bad_requests(engine):
+    from luxum_gb300 import LuxumError, Server
+
+    with Server() as srv:
+        p = _params("planar_oblique")
+        p.precision = 0
+        with pytest.raises(LuxumError):
+            srv.submit(p, 10)  # precision differs from the server's
+        q = _params("planar_oblique")
+        q.Nx = 2
+        with pytest.raises(LuxumError):
+            srv.submit(q, 10)  # reader::checkData-style rejection
