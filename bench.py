@@ -51,7 +51,7 @@ def workload_params(precision: int = 0, n: int = N):
                   usePW=1, kx_pw=1.0, ky_pw=0.0, kz_pw=0.0, Ex_pw=0.0, Ey_pw=0.0, Ez_pw=1.0, off_pw=24.0,
                   x1_pw=box[0], x2_pw=box[1], y1_pw=box[0], y2_pw=box[1], z1_pw=box[0], z2_pw=box[1],
                   usePML=1, d_pml=CPML * 1e-3, sigma=0.65, sigma_m=3.0, kappa=15.0, a_max=0.0, a_m=1.0,
-                  precision=precision, n_threads=os.cpu_count() or 1)
+                  precision=precision, n_threads=os.cpu_count() or 1, monitor_every=1)
 
 
 def profile_case(n: int, steps: int, precision: int) -> None:
@@ -452,6 +452,11 @@ def bench_phc(args):
             entry["field_rel_l2_vs_fp64"] = errs
             entry["T_max_abs_err_vs_fp64"] = float(np.nanmax(np.abs(T - ref[1])))
             entry["T_rel_l2_vs_fp64"] = float(np.sqrt(np.nansum((T - ref[1]) ** 2) / np.nansum(ref[1] ** 2)))
+            # the band where the input plane carries at least 1 % of its peak power (outside it
+            # T is a ratio of two small numbers)
+            band = np.abs(ref[2]) >= 0.01 * np.abs(ref[2]).max()
+            entry["T_max_abs_err_in_band"] = float(np.max(np.abs(T - ref[1])[band]))
+            entry["band_ghz"] = [float(PHC_OMEGA[band].min() / 2 / np.pi / 1e9), float(PHC_OMEGA[band].max() / 2 / np.pi / 1e9)]
             entry["flux_out_rel_l2_vs_fp64"] = float(np.linalg.norm(fout - ref[3]) / np.linalg.norm(ref[3]))
             entry["speedup_vs_fp64"] = out["fp64"]["seconds"] / dt
         out[name] = entry
@@ -530,7 +535,7 @@ def bench_reference(args):
 def config_dict(extra: str = ""):
     d = {"workload": f"3D Yee {N}^3 FP64, {STEPS} steps, CPML {CPML} (m=3, kappa 15), TF/SF x-wave box "
                      f"[{BOX[0]},{BOX[1]}]^3, eps_r 6 cube [{CUBE[0]},{CUBE[1]})^3, Ex..Hz snapshots every "
-                     f"{SNAP_EVERY} steps, 8 probes x 6 components every step",
+                     f"{SNAP_EVERY} steps, 8 probes x 6 components every step, max|E|^2 every step",
          "grid": [N, N, N], "time_steps_per_bench_step": STEPS, "cell_updates_per_bench_step": N ** 3 * STEPS,
          "l2": "no flush: resident state 5.4 GB >> 129 MB L2", "parallelism": "replicas (one independent sim per GPU)"}
     if extra:

@@ -179,6 +179,14 @@ LX_API lx_status lx_sim_read_field_noalloc(lx_sim* sim, int comp, double* host, 
 LX_API int lx_sim_timestep(const lx_sim* sim);
 /* max over the grid of Ey^2 (planar) or Ex^2+Ey^2+Ez^2 (3D) after the last monitor step. */
 LX_API lx_status lx_sim_max_e2(lx_sim* sim, double* out);
+/* The max|E|^2 of every monitored step (each step when monitor_every = 1; the last step of
+ * each lx_sim_step call otherwise), kept on the device without a host round trip per step:
+ * the series the reference drivers print, "t: <t>, max: <max>" (two_dim_pml.cc:135-141,
+ * three_dim_pml.cc:168-175).  Up to `capacity` entries are kept between reads; later steps
+ * still update lx_sim_max_e2 but are not recorded.  lx_sim_read_max_series returns the
+ * steps and values recorded since the last read (*rows of them) and empties the series. */
+LX_API lx_status lx_sim_set_max_series(lx_sim* sim, int capacity);
+LX_API lx_status lx_sim_read_max_series(lx_sim* sim, int* steps, double* max_e2, int capacity, int* rows);
 
 /* Point probes: every step records all six components at each (i,j,k) (0 where a
  * component's extent does not contain the index).  Replaces earlier probes. */
@@ -195,6 +203,15 @@ LX_API lx_status lx_sim_read_probes(lx_sim* sim, double* host, size_t n, int* ns
  * (0 outside a component's extent).  Planar grids: the plane is a line, axis 0 or 2. */
 LX_API lx_status lx_sim_add_dft_plane(lx_sim* sim, int axis, int index, int nfreq, const double* omega, int every,
                                       int* id);
+/* Checkpoint / resume.  lx_sim_save writes the handle's whole state to one HDF5 file:
+ * datasets "Ex".."Hz" in the layout of the snapshot files (staggered extents, C order,
+ * physical values), then the per-cell Cb, the CPML psi slabs, the DFT accumulators and the
+ * step counter.  lx_sim_load restores it into a handle created with the same parameters
+ * (the step count, thread and process counts and monitor cadence may differ) and the same
+ * DFT planes; the run then continues bit for bit as the saved one would have.  The probe
+ * series restarts empty.  No reference counterpart (the reference cannot resume). */
+LX_API lx_status lx_sim_save(lx_sim* sim, const char* path);
+LX_API lx_status lx_sim_load(lx_sim* sim, const char* path);
 /* Raw accumulators [nfreq][4][na][nb][2] (re, im), (na, nb) = in-plane extents in axis order. */
 LX_API lx_status lx_sim_read_dft(lx_sim* sim, int id, double* host, size_t n);
 /* Net power flux through the plane per frequency: sum over cells of

@@ -114,6 +114,10 @@ def declare(lib) -> None:
     _proto(lib, "lx_sim_read_probes", C.c_int, sim, P(C.c_double), C.c_size_t, P(C.c_int))
     _proto(lib, "lx_sim_add_dft_plane", C.c_int, sim, C.c_int, C.c_int, C.c_int, P(C.c_double), C.c_int, P(C.c_int))
     _proto(lib, "lx_sim_read_dft", C.c_int, sim, C.c_int, P(C.c_double), C.c_size_t)
+    _proto(lib, "lx_sim_save", C.c_int, sim, C.c_char_p)
+    _proto(lib, "lx_sim_set_max_series", C.c_int, sim, C.c_int)
+    _proto(lib, "lx_sim_read_max_series", C.c_int, sim, P(C.c_int), P(C.c_double), C.c_int, P(C.c_int))
+    _proto(lib, "lx_sim_load", C.c_int, sim, C.c_char_p)
     _proto(lib, "lx_sim_dft_flux", C.c_int, sim, C.c_int, P(C.c_double), C.c_int)
     _proto(lib, "lx_sim_set_snapshots", C.c_int, sim, C.c_int, C.c_uint, SNAPSHOT_FN, C.c_void_p)
     _proto(lib, "lx_sim_set_hdf5_output", C.c_int, sim, C.c_int, C.c_int, C.c_int, C.c_char_p)

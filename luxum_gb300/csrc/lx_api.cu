@@ -376,7 +376,7 @@ extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
     for (int q = 0; q < 6; q++) dfree(s->prof[c][q], fs);
     for (int q = 0; q < 2; q++) { dfree(s->psiH[c][q], fs); dfree(s->psiE[c][q], fs); }
   }
-  dfree(s->tab, fs); dfree(s->d_max, fs); dfree(s->etotal, fs); dfree(s->xfer, fs);
+  dfree(s->tab, fs); dfree(s->d_max, fs); dfree(s->d_series, fs); dfree(s->etotal, fs); dfree(s->xfer, fs);
   dfree(s->d_probe_ijk, fs); dfree(s->d_probe, fs);
   for (auto& sl : s->slots) {
     dfree(sl.dev, fs);
@@ -566,6 +566,7 @@ extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
   if (!s) return fail(nullptr, LX_ERR_OOM, "host allocation failed");
   keep_pool_memory();
   setup_host(s, p);
+  cudaGetDevice(&s->device);
 
   cudaError_t e = cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
@@ -639,6 +640,7 @@ extern "C" LX_API lx_status lx_sim_reset(lx_sim* s) {
   for (auto& d : s->dfts) CK(cudaMemsetAsync(d.d_acc, 0, d.n_acc * sizeof(double), s->stream));
   s->t = 0;
   s->probe_rows = 0;
+  s->series_t.clear();
   s->last_max = 0.0;
   return LX_OK;
 }
@@ -736,6 +738,174 @@ extern "C" LX_API lx_status lx_sim_write_field(lx_sim* s, int comp, const double
   const bool hcomp = comp >= LX_HX && comp <= LX_HZ;
   if ((st = scatter(s, comp, comp_ptr(s, comp), false, hcomp && s->hscale != 1.0 ? 1 : 0, s->hscale, 0.0))) return st;
   CK(cudaStreamSynchronize(s->stream));
+  return LX_OK;
+}
+
+// ------------------------------------------------------------------ checkpoints
+
+namespace {
+const char* kCompName[6] = {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz"};
+
+// lx_params with the members a resumed run may change (step count, threads, decomposition,
+// monitor cadence) cleared, for the compatibility check.
+std::vector<double> params_key(const lx_params& p0) {
+  lx_params p = p0;
+  p.num_timesteps = 0;
+  p.n_threads = 0;
+  p.npX = p.npY = 0;
+  p.monitor_every = 0;
+  std::vector<double> v((sizeof(lx_params) + 7) / 8, 0.0);
+  std::memcpy(v.data(), &p, sizeof p);
+  return v;
+}
+
+// raw device array of compute-precision values <-> doubles on the host
+lx_status raw_to_host(lx_sim* s, const void* dev, size_t n, std::vector<double>& out) {
+  out.resize(n);
+  if (!n) return LX_OK;
+  if (s->csize == 8) {
+    CK(cudaMemcpyAsync(out.data(), dev, n * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+  } else {
+    std::vector<float> f(n);
+    CK(cudaMemcpyAsync(f.data(), dev, n * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    for (size_t q = 0; q < n; q++) out[q] = f[q];
+  }
+  s->n_d2h += n * s->csize;
+  return LX_OK;
+}
+
+lx_status raw_to_device(lx_sim* s, void* dev, const std::vector<double>& in) {
+  const size_t n = in.size();
+  if (!n) return LX_OK;
+  if (s->csize == 8) {
+    CK(cudaMemcpyAsync(dev, in.data(), n * 8, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+  } else {
+    std::vector<float> f(n);
+    for (size_t q = 0; q < n; q++) f[q] = (float)in[q];
+    CK(cudaMemcpyAsync(dev, f.data(), n * 4, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  s->n_h2d += n * s->csize;
+  return LX_OK;
+}
+}  // namespace
+
+extern "C" LX_API lx_status lx_sim_save(lx_sim* s, const char* path) {
+  if (!s || !path) return fail(s, LX_ERR_INVALID, "null argument");
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  if ((st = ensure_xfer(s))) return st;
+  lx::Hdf5Writer w;
+  std::string m = w.open(path, s->ext[LX_EY]);
+  if (!m.empty()) return fail(s, LX_ERR_IO, m);
+  std::vector<double> host;
+  auto put = [&](const std::string& name, const std::vector<double>& v, const int* ext) -> lx_status {
+    const std::string e = w.write_named(name, v.data(), ext);
+    return e.empty() ? LX_OK : fail(s, LX_ERR_IO, e);
+  };
+  // fields in the snapshot layout (physical values, staggered extents, C order)
+  for (int c = 0; c < 6; c++) {
+    const size_t n = ext_n(s, c);
+    if (!n) continue;
+    host.resize(n);
+    if ((st = lx_sim_read_field(s, c, host.data(), n))) return st;
+    if ((st = put(kCompName[c], host, s->ext[c]))) return st;
+  }
+  // per-cell coefficients as stored (Cb in the engine's units)
+  for (int c = 0; c < 3; c++) {
+    const size_t n = ext_n(s, c);
+    if (!n) continue;
+    if (s->csize == 8) CK(lx::launch_gather<double>((const double*)s->Cbs[c], s->xfer, s->ext[c], s->Ny, s->Nzp, 1.0, s->stream));
+    else CK(lx::launch_gather<float>((const float*)s->Cbs[c], s->xfer, s->ext[c], s->Ny, s->Nzp, 1.0, s->stream));
+    host.resize(n);
+    CK(cudaMemcpyAsync(host.data(), s->xfer, n * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if ((st = put(std::string("Cb_") + kCompName[c], host, s->ext[c]))) return st;
+  }
+  // CPML psi on the slabs and DFT accumulators, raw
+  for (int a = 0; a < 3; a++)
+    for (int q = 0; q < 2; q++) {
+      for (int h = 0; h < 2; h++) {
+        const size_t n = h ? s->psiH_n[a][q] : s->psiE_n[a][q];
+        if (!n) continue;
+        if ((st = raw_to_host(s, h ? s->psiH[a][q] : s->psiE[a][q], n, host))) return st;
+        const int ext[3] = {1, 1, (int)n};
+        if ((st = put(std::string(h ? "psiH_" : "psiE_") + char('0' + a) + char('0' + q), host, ext))) return st;
+      }
+    }
+  for (size_t d = 0; d < s->dfts.size(); d++) {
+    const lx::DftPlane& D = s->dfts[d];
+    host.resize(D.n_acc);
+    CK(cudaMemcpyAsync(host.data(), D.d_acc, D.n_acc * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const int ext[3] = {1, 1, (int)D.n_acc};
+    if ((st = put("dft_" + std::to_string(d), host, ext))) return st;
+  }
+  const std::vector<double> state = {(double)s->t, s->last_max, (double)s->prec, (double)s->dfts.size()};
+  const int sext[3] = {1, 1, (int)state.size()};
+  if ((st = put("engine_state", state, sext))) return st;
+  const std::vector<double> key = params_key(s->p);
+  const int kext[3] = {1, 1, (int)key.size()};
+  if ((st = put("engine_params", key, kext))) return st;
+  m = w.close();
+  if (!m.empty()) return fail(s, LX_ERR_IO, m);
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_load(lx_sim* s, const char* path) {
+  if (!s || !path) return fail(s, LX_ERR_INVALID, "null argument");
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  std::vector<double> v;
+  int shp[3];
+  auto get = [&](const std::string& name, size_t n) -> lx_status {
+    const std::string e = lx::hdf5_read(path, name.c_str(), v, shp);
+    if (!e.empty()) return fail(s, LX_ERR_IO, name + ": " + e);
+    if (v.size() != n) return fail(s, LX_ERR_INVALID, name + ": size does not match this handle");
+    return LX_OK;
+  };
+  const std::vector<double> key = params_key(s->p);
+  if ((st = get("engine_params", key.size()))) return st;
+  if (std::memcmp(v.data(), key.data(), key.size() * 8) != 0)
+    return fail(s, LX_ERR_INVALID, "checkpoint was written by a handle with other parameters");
+  if ((st = get("engine_state", 4))) return st;
+  const std::vector<double> state = v;
+  if ((int)state[2] != s->prec) return fail(s, LX_ERR_INVALID, "checkpoint precision differs");
+  if ((size_t)state[3] != s->dfts.size()) return fail(s, LX_ERR_INVALID, "checkpoint has another number of DFT planes");
+  for (size_t d = 0; d < s->dfts.size(); d++)
+    if ((st = get("dft_" + std::to_string(d), s->dfts[d].n_acc))) return st;
+  for (int c = 0; c < 6; c++) {
+    const size_t n = ext_n(s, c);
+    if (!n) continue;
+    if ((st = get(kCompName[c], n))) return st;
+    if ((st = lx_sim_write_field(s, c, v.data(), n))) return st;
+  }
+  for (int c = 0; c < 3; c++) {
+    const size_t n = ext_n(s, c);
+    if (!n) continue;
+    if ((st = get(std::string("Cb_") + kCompName[c], n))) return st;
+    if ((st = upload(s, v.data(), n))) return st;
+    if ((st = scatter(s, c, s->Cbs[c], true, 0, 1.0, 0.0))) return st;
+  }
+  for (int a = 0; a < 3; a++)
+    for (int q = 0; q < 2; q++)
+      for (int h = 0; h < 2; h++) {
+        const size_t n = h ? s->psiH_n[a][q] : s->psiE_n[a][q];
+        if (!n) continue;
+        if ((st = get(std::string(h ? "psiH_" : "psiE_") + char('0' + a) + char('0' + q), n))) return st;
+        if ((st = raw_to_device(s, h ? s->psiH[a][q] : s->psiE[a][q], v))) return st;
+      }
+  for (size_t d = 0; d < s->dfts.size(); d++) {
+    if ((st = get("dft_" + std::to_string(d), s->dfts[d].n_acc))) return st;
+    CK(cudaMemcpyAsync(s->dfts[d].d_acc, v.data(), v.size() * 8, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  s->t = (int)state[0];
+  s->last_max = state[1];
+  s->probe_rows = 0;
   return LX_OK;
 }
 
@@ -888,7 +1058,7 @@ extern "C" LX_API lx_status lx_sim_dft_flux(lx_sim* s, int id, double* flux, int
 // ------------------------------------------------------------------ snapshots
 
 static void writer_main(lx_sim* s) {
-  cudaSetDevice(0);
+  cudaSetDevice(s->device);
   for (;;) {
     lx::SnapJob job;
     {
@@ -1173,6 +1343,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
   prb.ijk = s->d_probe_ijk;
   prb.hmul = 1.0 / s->hscale;
 
+  unsigned long long* last_slot = s->d_max;
   for (int q = 0; q < nsteps; q++) {
     const int t = s->t;
     bool mon = (q == nsteps - 1) || (s->p.monitor_every > 0 && (t + 1) % s->p.monitor_every == 0);
@@ -1194,9 +1365,15 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
       return LX_OK;
     };
     lx_status st;
+    unsigned long long* slot = s->d_max;
+    if (mon && s->d_series && (int)s->series_t.size() < s->series_cap) {
+      slot = s->d_series + s->series_t.size();
+      s->series_t.push_back(t);
+    }
+    if (mon) last_slot = slot;
     if (pp.tab_total > 0 || s->src_kind >= 0 || mon) {
       pp.t = t;
-      pp.max_slot = mon ? s->d_max : nullptr;
+      pp.max_slot = mon ? slot : nullptr;
       if ((st = tic())) return st;
       if (s->csize == 8) CK(lx::launch_prologue<double>(pp, s->stream));
       else CK(lx::launch_prologue<float>(pp, s->stream));
@@ -1206,7 +1383,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
     if ((st = tic())) return st;
     CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, true, s->stream));
     if ((st = toc(1))) return st;
-    sp.max_slot = mon ? s->d_max : nullptr;
+    sp.max_slot = mon ? slot : nullptr;
     sp.etotal = (snap & (1u << LX_ETOTAL)) ? (C*)s->etotal : nullptr;
     if ((st = tic())) return st;
     CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, false, s->stream));
@@ -1242,7 +1419,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
   }
   if (nsteps > 0) {
     unsigned long long bits = 0;
-    CK(cudaMemcpyAsync(&bits, s->d_max, sizeof bits, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(&bits, last_slot, sizeof bits, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     s->n_d2h += sizeof bits;
     double v;
@@ -1291,6 +1468,43 @@ extern "C" LX_API lx_status lx_sim_time_kernels(lx_sim* s, int nsteps, double ou
 }
 
 extern "C" LX_API int lx_sim_timestep(const lx_sim* s) { return s ? s->t : -1; }
+
+extern "C" LX_API lx_status lx_sim_set_max_series(lx_sim* s, int capacity) {
+  if (!s || capacity < 0) return fail(s, LX_ERR_INVALID, "capacity must be >= 0");
+  if (s->batch) return fail(s, LX_ERR_STATE, "batched members keep no max series");
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  dfree(s->d_series, s->own);
+  s->d_series = nullptr;
+  s->series_cap = 0;
+  s->series_t.clear();
+  if (capacity > 0) {
+    CK(cudaMallocAsync(&s->d_series, sizeof(unsigned long long) * capacity, s->own));
+    CK(cudaStreamSynchronize(s->own));
+    s->series_cap = capacity;
+  }
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_sim_read_max_series(lx_sim* s, int* steps, double* values, int capacity, int* rows) {
+  if (!s || !rows) return fail(s, LX_ERR_INVALID, "null argument");
+  lx_status st = lx_sim_sync(s);
+  if (st) return st;
+  const int n = (int)s->series_t.size();
+  *rows = n;
+  if (n == 0) return LX_OK;
+  if (!steps || !values || capacity < n) return fail(s, LX_ERR_INVALID, "buffers hold fewer entries than the series");
+  std::vector<unsigned long long> bits(n);
+  CK(cudaMemcpyAsync(bits.data(), s->d_series, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_d2h += sizeof(unsigned long long) * n;
+  for (int q = 0; q < n; q++) {
+    steps[q] = s->series_t[q];
+    std::memcpy(&values[q], &bits[q], sizeof(double));
+  }
+  s->series_t.clear();
+  return LX_OK;
+}
 
 extern "C" LX_API lx_status lx_sim_max_e2(lx_sim* s, double* out) {
   if (!s || !out) return fail(s, LX_ERR_INVALID, "null argument");
@@ -1471,8 +1685,8 @@ extern "C" LX_API lx_status lx_batch_add(lx_batch* b, lx_sim* s) {
   if (st) return st;
   if (s->batch) return bfail(b, LX_ERR_INVALID, s->batch == b ? "handle already in this batch" : "handle is in another batch");
   if (b->prec >= 0 && s->prec != b->prec) return bfail(b, LX_ERR_INVALID, "all members of a batch share one precision");
-  if (!s->outputs.empty() || s->nprobes > 0)
-    return bfail(b, LX_ERR_UNSUPPORTED, "batched members cannot have snapshot outputs or probes");
+  if (!s->outputs.empty() || s->nprobes > 0 || s->d_series)
+    return bfail(b, LX_ERR_UNSUPPORTED, "batched members cannot have snapshot outputs, probes or a max series");
   if ((st = lx_sim_sync(s))) return st;
   b->prec = s->prec;
   b->sims.push_back(s);

@@ -92,11 +92,13 @@ std::string Hdf5Writer::open(const char* path, const int ext[3]) {
 
 std::string Hdf5Writer::write(int t, const double* data) { return write_named(dataset_name(t), data); }
 
-std::string Hdf5Writer::write_named(const std::string& name, const double* data) {
+std::string Hdf5Writer::write_named(const std::string& name, const double* data, const int* ext) {
   if (!f_) return "HDF5 file is not open";
-  const uint64_t n = (uint64_t)ext_[0] * ext_[1] * ext_[2];
+  if (!ext) ext = ext_;
+  const uint64_t n = (uint64_t)ext[0] * ext[1] * ext[2];
   Entry e;
   e.name = name;
+  for (int a = 0; a < 3; a++) e.ext[a] = ext[a];
   e.addr = eof_;
   e.bytes = n * 8;
   if (std::fseek(f_, (long)eof_, SEEK_SET) != 0) return "seek failed";
@@ -134,7 +136,7 @@ std::string Hdf5Writer::close() {
   for (auto& e : ents) {
     std::vector<uint8_t> msgs, d;
     d = {1, 3, 0, 0, 0, 0, 0, 0};  // dataspace v1, rank 3, no max dims
-    for (int a = 0; a < 3; a++) put64(d, (uint64_t)ext_[a]);
+    for (int a = 0; a < 3; a++) put64(d, (uint64_t)e.ext[a]);
     message(msgs, 0x0001, d);
     d = {0x11, 0x20, 63, 0};  // datatype v1 class float: LE, implied msb, sign bit 63
     put32(d, 8);

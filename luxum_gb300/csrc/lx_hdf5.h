@@ -6,19 +6,22 @@
 
 namespace lx {
 
-// Appends one 3-D native-double dataset "t=<step>" per write to a single file.
+// Appends one 3-D native-double dataset "t=<step>" per write to a single file (or named
+// datasets of their own extents: checkpoints).
 class Hdf5Writer {
  public:
   ~Hdf5Writer();
   std::string open(const char* path, const int ext[3]);
   std::string write(int t, const double* data);  // dataset "t=<t>" (fileio.cc:186-187)
-  std::string write_named(const std::string& name, const double* data);
+  // ext: this dataset's extents (nullptr: the file's, from open)
+  std::string write_named(const std::string& name, const double* data, const int* ext = nullptr);
   std::string close();
 
  private:
   struct Entry {
     std::string name;
     unsigned long long addr, bytes;
+    int ext[3];
   };
   std::FILE* f_ = nullptr;
   int ext_[3] = {0, 0, 0};

@@ -192,31 +192,50 @@ __global__ void tick_kernel(int* ts, int n) {
 
 // ------------------------------------------------------------------ monitor
 
-__device__ __forceinline__ void block_max_atomic(unsigned long long v, unsigned long long* slot) {
-  __shared__ unsigned long long red[32];
+// max|E|^2 is reduced on bit patterns: squares are non-negative, so their IEEE patterns
+// order like their values, and NaN/inf sort above every finite value (blow-up detection).
+// FP32 members reduce 32-bit float patterns and widen only the block's winner to the
+// double pattern the monitor slot holds.
+template <class C>
+struct MaxBits;
+template <>
+struct MaxBits<double> {
+  using type = unsigned long long;
+  static __device__ __forceinline__ type of(double v) { return (unsigned long long)__double_as_longlong(v); }
+};
+template <>
+struct MaxBits<float> {
+  using type = unsigned;
+  static __device__ __forceinline__ type of(float v) { return __float_as_uint(v); }
+};
+
+__device__ __forceinline__ unsigned long long as_slot_bits(unsigned long long v) { return v; }
+__device__ __forceinline__ unsigned long long as_slot_bits(unsigned v) {
+  return (unsigned long long)__double_as_longlong((double)__uint_as_float(v));
+}
+__device__ __forceinline__ unsigned long long warp_max(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
     v = w > v ? w : v;
   }
+  return v;
+}
+__device__ __forceinline__ unsigned warp_max(unsigned v) { return __reduce_max_sync(0xffffffffu, v); }
+
+// Block maximum of the bit patterns, then one atomicMax on the 64-bit slot per block.
+template <class B>
+__device__ __forceinline__ void block_max_atomic(B v, unsigned long long* slot) {
+  __shared__ B red[32];
+  v = warp_max(v);
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int nw = (blockDim.x * blockDim.y + 31) / 32;
   if ((tid & 31) == 0) red[tid >> 5] = v;
   __syncthreads();
   if (tid < 32) {
-    v = tid < nw ? red[tid] : 0ull;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-      v = w > v ? w : v;
-    }
-    if (tid == 0 && v) atomicMax(slot, v);
+    v = warp_max(tid < nw ? red[tid] : B(0));
+    if (tid == 0 && v) atomicMax(slot, as_slot_bits(v));
   }
-}
-
-__device__ __forceinline__ unsigned long long e2_bits(double v) { return (unsigned long long)__double_as_longlong(v); }
-__device__ __forceinline__ unsigned long long e2_bits(float v) {
-  return (unsigned long long)__double_as_longlong((double)v);
 }
 
 // ------------------------------------------------------------------ 3-D kernels
@@ -307,8 +326,8 @@ __global__ void __launch_bounds__(256) h_kernel_3d(const StepParams<T, C> p) {
 // index in [1, N-2]) change; on the PEC walls the reference adds Cb*0 and psi stays 0.
 // Returns the bit pattern of this cell's |E|^2 when monitoring (0 otherwise).
 template <class T, class C, bool UNI, bool MON>
-__device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k,
-                                                        const bool tf) {
+__device__ __forceinline__ typename MaxBits<C>::type e_cell_3d(const StepParams<T, C>& p, const int i, const int j,
+                                                               const int k, const bool tf) {
   const long long c = (long long)i * p.si + (long long)j * p.sj + k;
   const bool ii = (i >= 1 && i < p.Nx - 1), jj = (j >= 1 && j < p.Ny - 1), kk = (k >= 1 && k < p.Nz - 1);
   const bool ux = (i < p.Nx - 1 && jj && kk), uy = (ii && j < p.Ny - 1 && kk), uz = (ii && jj && k < p.Nz - 1);
@@ -367,12 +386,12 @@ __device__ __forceinline__ unsigned long long e_cell_3d(const StepParams<T, C>& 
   if (ux) st<T, C>(p.E[0] + c, exn);
   if (uy) st<T, C>(p.E[1] + c, eyn);
   if (uz) st<T, C>(p.E[2] + c, ezn);
-  unsigned long long mbits = 0ull;
+  typename MaxBits<C>::type mbits = 0;
   if (mon) {
     // Etotal = Ez*Ez + Ey*Ey + Ex*Ex (three_dim_pml.cc:270), same association order
     const C e2 = fmaC(exn, exn, fmaC(eyn, eyn, ezn * ezn));
     if (p.etotal) p.etotal[c] = e2;
-    mbits = e2_bits(e2);
+    mbits = MaxBits<C>::of(e2);
   }
   return mbits;
 }
@@ -383,7 +402,7 @@ __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
   const int j = blockIdx.y * 8 + threadIdx.y;
   const int i0 = blockIdx.z * M;
   const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, M, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
-  unsigned long long mbits = 0ull;
+  typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz && j < p.Ny) {
     if constexpr (M == 1) {
       mbits = e_cell_3d<T, C, UNI, MON>(p, i0, j, k, tf);
@@ -391,7 +410,7 @@ __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
       const int i1 = min(i0 + M, p.Nx);
 #pragma unroll 1
       for (int i = i0; i < i1; ++i) {
-        const unsigned long long b = e_cell_3d<T, C, UNI, MON>(p, i, j, k, tf);
+        const typename MaxBits<C>::type b = e_cell_3d<T, C, UNI, MON>(p, i, j, k, tf);
         mbits = b > mbits ? b : mbits;
       }
     }
@@ -454,7 +473,7 @@ __global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
 // covers i < Nx-1, k < Nz-1, but its H-curl is only computed for i, k in [1, N-2]
 // (vfield.cc:376-381), so the other cells add Cb*0 and are skipped here.
 template <class T, class C, bool UNI, bool MON>
-__device__ __forceinline__ unsigned long long e_cell_2d(const StepParams<T, C>& p, const int i, const int k,
+__device__ __forceinline__ typename MaxBits<C>::type e_cell_2d(const StepParams<T, C>& p, const int i, const int k,
                                                         const bool tf) {
   const long long c = (long long)i * p.si + k;
   const bool u = (i >= 1 && i < p.Nx - 1 && k >= 1 && k < p.Nz - 1);
@@ -480,7 +499,7 @@ __device__ __forceinline__ unsigned long long e_cell_2d(const StepParams<T, C>& 
     st<T, C>(p.E[1] + c, eyn);
   }
   // local_max = max(Ey*Ey) over the whole Ey array (two_dim_pml.cc:181)
-  return MON ? e2_bits(eyn * eyn) : 0ull;
+  return MON ? MaxBits<C>::of(eyn * eyn) : typename MaxBits<C>::type(0);
 }
 
 template <class T, class C, bool UNI, bool MON, int M>
@@ -488,13 +507,13 @@ __global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int ib = blockIdx.y * 8 * M;
   const bool tf = p.tfsf && tile_meets_planes(p.planesE, ib, 8 * M, 0, 1, blockIdx.x * 32, 32);
-  unsigned long long mbits = 0ull;
+  typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz) {
 #pragma unroll 1
     for (int r = 0; r < M; ++r) {
       const int i = ib + threadIdx.y + 8 * r;
       if (i < p.Nx) {
-        const unsigned long long b = e_cell_2d<T, C, UNI, MON>(p, i, k, tf);
+        const typename MaxBits<C>::type b = e_cell_2d<T, C, UNI, MON>(p, i, k, tf);
         mbits = b > mbits ? b : mbits;
       }
     }
@@ -562,12 +581,12 @@ __global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __rest
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x, j = tl.z + threadIdx.y, i0 = tl.y;
   const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, kMarch, tl.z, 8, tl.w, 32);
-  unsigned long long mbits = 0ull;
+  typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz && j < p.Ny) {
     const int i1 = min(i0 + kMarch, p.Nx);
 #pragma unroll 1
     for (int i = i0; i < i1; ++i) {
-      const unsigned long long b = e_cell_3d<T, C, UNI, true>(p, i, j, k, tf);
+      const typename MaxBits<C>::type b = e_cell_3d<T, C, UNI, true>(p, i, j, k, tf);
       mbits = b > mbits ? b : mbits;
     }
   }
@@ -595,13 +614,13 @@ __global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __rest
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x;
   const bool tf = p.tfsf && tile_meets_planes(p.planesE, tl.y, 8 * kMarch, 0, 1, tl.w, 32);
-  unsigned long long mbits = 0ull;
+  typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz) {
 #pragma unroll 1
     for (int r = 0; r < kMarch; ++r) {
       const int i = tl.y + threadIdx.y + 8 * r;
       if (i < p.Nx) {
-        const unsigned long long b = e_cell_2d<T, C, UNI, true>(p, i, k, tf);
+        const typename MaxBits<C>::type b = e_cell_2d<T, C, UNI, true>(p, i, k, tf);
         mbits = b > mbits ? b : mbits;
       }
     }

@@ -10,8 +10,9 @@
 //            GPU runs -> lx_batch_wait -> retire finished / failed / cancelled requests
 //
 // The chunk is the server's chunk, shortened so that no running request passes its step
-// count.  Built only on the public C ABI (luxum.h) plus cudaMemGetInfo for the default
-// budget.
+// count.  Built only on the public C ABI (luxum.h) plus the CUDA runtime for the default
+// budget and the device: a server runs on the device current at its creation (one server
+// per GPU for several GPUs).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -70,6 +71,7 @@ struct lx_server {
   std::vector<std::shared_ptr<Request>> running;   // members of the batch
   std::vector<std::shared_ptr<Request>> prepared;  // handles created, not yet in the batch
   long long next_id = 1;
+  int device = 0;  // CUDA device current at lx_server_create; the worker runs on it
   bool stop = false;
   lx_batch* batch = nullptr;
   lx_server_stats stats;
@@ -217,6 +219,7 @@ void retire(lx_server* srv) {
 }
 
 void worker_main(lx_server* srv) {
+  cudaSetDevice(srv->device);
   for (;;) {
     prepare(srv);
     int n = 0;
@@ -317,6 +320,7 @@ extern "C" LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_ser
   if (!srv) return sfail(LX_ERR_OOM, "host allocation failed");
   srv->cfg = c;
   srv->t0 = Clock::now();
+  cudaGetDevice(&srv->device);
   std::memset(&srv->stats, 0, sizeof srv->stats);
   lx_status st = lx_batch_create(&srv->batch);
   if (!st) st = lx_batch_set_chunk(srv->batch, c.chunk);

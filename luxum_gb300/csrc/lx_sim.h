@@ -65,6 +65,7 @@ struct Consts {
 struct lx_sim {
   lx_params p;
   lx_batch* batch = nullptr;  // the batch this handle is a member of
+  int device = 0;             // CUDA device current when the handle was created
   lx::Consts k;
   std::string err;
   int planar = 0, pml = 0, uniform = 0, prec = 0, tfsf = 0;
@@ -86,6 +87,10 @@ struct lx_sim {
   int tab_total = 0;
   lx::PatchSet setsH[3][2] = {}, setsE[3][2] = {};
   unsigned long long* d_max = nullptr;
+  // max|E|^2 series: one slot per monitored step (device), the step of each slot (host)
+  unsigned long long* d_series = nullptr;
+  int series_cap = 0;
+  std::vector<int> series_t;
   void* etotal = nullptr;
   double* xfer = nullptr;  // compact staging for field/material transfers
   size_t xfer_cap = 0;

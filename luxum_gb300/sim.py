@@ -223,6 +223,29 @@ class Sim:
         self._cb = _ffi.SNAPSHOT_FN(trampoline)
         self._check(self.lib.lx_sim_set_snapshots(self.h, every, mask, self._cb, None))
 
+    def set_max_series(self, capacity: int) -> None:
+        """Keep max|E|^2 of every monitored step on the device (up to capacity between reads)."""
+        self._check(self.lib.lx_sim_set_max_series(self.h, capacity))
+        self._series_cap = capacity
+
+    def max_series(self):
+        """(steps, max|E|^2) recorded since the last call; empties the series."""
+        cap = max(getattr(self, "_series_cap", 0), 1)
+        ts = np.empty(cap, dtype=np.int32)
+        vs = np.empty(cap)
+        rows = C.c_int()
+        self._check(self.lib.lx_sim_read_max_series(self.h, ts.ctypes.data_as(C.POINTER(C.c_int)),
+                                                     vs.ctypes.data_as(C.POINTER(C.c_double)), cap, C.byref(rows)))
+        return ts[: rows.value].copy(), vs[: rows.value].copy()
+
+    def save(self, path: str) -> None:
+        """Checkpoint: the whole state into one HDF5 file (fields as in the snapshot files)."""
+        self._check(self.lib.lx_sim_save(self.h, str(path).encode()))
+
+    def load(self, path: str) -> None:
+        """Resume from a checkpoint written by a handle with the same parameters and DFT planes."""
+        self._check(self.lib.lx_sim_load(self.h, str(path).encode()))
+
     def set_hdf5_output(self, every: int, comp: int, path: str, first: int = 0) -> None:
         self._check(self.lib.lx_sim_set_hdf5_output(self.h, every, first, comp, str(path).encode()))
 

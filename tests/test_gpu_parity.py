@@ -172,3 +172,61 @@ def test_blowup_is_reported(engine):
     with pytest.raises(LuxumError) as ei:
         g.step(2)
     assert ei.value.status == 5
+
+
+@pytest.mark.parametrize("scale", ["mixed", "tiny", "huge", "sparse_denormal"])
+def test_max_monitor_equals_etotal_max(engine, scale):
+    """The max|E|^2 monitor (a block reduction on bit patterns, then atomicMax) equals, bit for
+    bit, the maximum of the |E|^2 array a twin keeps, for values from subnormal to huge."""
+    from luxum_gb300 import ETOTAL, Sim
+
+    p, _, _ = cases.build("3d_pml_axis")
+    rng = np.random.default_rng({"mixed": 1, "tiny": 2, "huge": 3, "sparse_denormal": 4}[scale])
+    a, b = Sim(p), Sim(p)
+    for c in range(6):
+        shp = a.shape(c)
+        if scale == "mixed":  # magnitudes 1e-300 .. 1e30 side by side
+            v = rng.standard_normal(shp) * 10.0 ** rng.uniform(-300, 30, shp)
+        elif scale == "tiny":  # squares below float's normal range
+            v = rng.standard_normal(shp) * 1e-25
+        elif scale == "huge":  # squares beyond float's range
+            v = rng.standard_normal(shp) * 1e25
+        else:  # zeros with a few subnormal doubles
+            v = np.zeros(shp)
+            idx = tuple(rng.integers(0, n, 5) for n in shp)
+            v[idx] = 1e-310
+        a.set_field(c, v)
+        b.set_field(c, v)
+    got = []
+    b.set_snapshots(1, 1 << ETOTAL, lambda t, comp, arr: got.append(arr.max()))
+    for _ in range(3):
+        a.step(1)
+        b.step(1)
+        b.sync()
+        assert a.max_e2() == b.max_e2() == got[-1]
+
+
+@pytest.mark.parametrize("name", ["planar_pml_axis", "3d_pml_axis"])
+def test_max_series_matches_oracle(engine, name):
+    """monitor_every = 1 with a device series: every step's max|E|^2, read once per chunk."""
+    from luxum_gb300 import Sim
+    from oracle.oracle import OracleSim
+
+    p, steps, boxes = cases.build(name)
+    p.monitor_every = 1
+    g, o = Sim(p), OracleSim(p, threads=4)
+    for lo, hi, eps in boxes:
+        g.set_eps_box(lo, hi, eps)
+        o.set_eps_box(lo, hi, eps)
+    g.set_max_series(25)
+    got_t, got_v = [], []
+    for _ in range(3):
+        g.step(20)
+        t, v = g.max_series()
+        got_t += list(t)
+        got_v += list(v)
+    assert got_t == list(range(60))
+    for t in range(60):
+        o.step(1)
+        assert got_v[t] == pytest.approx(o.max_e2(), rel=1e-11, abs=1e-300), t
+    assert got_v[-1] == g.max_e2()
