@@ -164,7 +164,8 @@ def kernel_model(sim, p):
     Bytes: every array a kernel must touch, once: H kernel reads E (3) and H (3) and writes
     H (3); E kernel reads H (3), E (3), Cb (3) and writes E (3); each stored psi entry is
     read and written once.  Flops per component: 3 differences + 1 FMA (5 flops); per psi
-    term: psi = b*psi + c*d and d/kappa + psi (5 flops).
+    term: psi = b*psi + c*d and d/kappa + psi (5 flops); with the max monitor every step the
+    E kernel also forms |E|^2 = Ex^2 + Ey^2 + Ez^2 per cell (5 flops, no extra bytes).
     """
     info = sim.info()
     el = info["field_bytes"]
@@ -174,7 +175,7 @@ def kernel_model(sim, p):
     h_bytes = cells * 9 * el + psi_h * 2 * cel
     e_bytes = cells * 9 * el + cells * 3 * cel + psi_e * 2 * cel
     h_flops = cells * 15 + psi_h * 5
-    e_flops = cells * 15 + psi_e * 5
+    e_flops = cells * 15 + psi_e * 5 + (cells * 5 if p.monitor_every == 1 else 0)
     return {"h_update": (h_bytes, h_flops), "e_update": (e_bytes, e_flops)}
 
 
