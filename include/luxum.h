@@ -159,6 +159,8 @@ LX_API lx_status lx_sim_sync(lx_sim* sim);
 
 /* Staggered extents of a component (field.cc:67-77); absent planar components give 0s. */
 LX_API lx_status lx_sim_field_shape(const lx_sim* sim, int comp, int shape[3]);
+/* The same for the handle *p would give, on the host without a GPU (validates *p). */
+LX_API lx_status lx_params_field_shape(const lx_params* p, int comp, int shape[3]);
 LX_API lx_status lx_sim_read_field(lx_sim* sim, int comp, double* host, size_t n);
 LX_API lx_status lx_sim_write_field(lx_sim* sim, int comp, const double* host, size_t n);
 /* Same result as lx_sim_read_field, but the call allocates nothing: no cudaMalloc, cudaFree
@@ -292,6 +294,11 @@ LX_API void lx_server_config_init(lx_server_config* cfg);
 typedef struct lx_request {
   lx_params params;       /* params.precision must equal the server's */
   int steps;              /* time steps to run */
+  /* material arrays F of E components LX_EX..LX_EZ (NULL: vacuum), each the component's
+   * staggered extent in C order; Cb = dt/(eps0*(1+F*material_scale)) (lx_sim_set_material),
+   * applied before the boxes */
+  const double* material[3];
+  double material_scale;
   int n_boxes;            /* dielectric boxes, applied in order (lx_sim_set_eps_box) */
   const int* boxes;       /* n_boxes x {lo[3], hi[3]} */
   const double* box_eps;  /* n_boxes relative permittivities */

@@ -66,7 +66,8 @@ class ServerConfig(C.Structure):
 
 
 class Request(C.Structure):
-    _fields_ = [("params", Params), ("steps", C.c_int), ("n_boxes", C.c_int), ("boxes", C.POINTER(C.c_int)),
+    _fields_ = [("params", Params), ("steps", C.c_int), ("material", C.POINTER(C.c_double) * 3),
+                ("material_scale", C.c_double), ("n_boxes", C.c_int), ("boxes", C.POINTER(C.c_int)),
                 ("box_eps", C.POINTER(C.c_double)), ("dft_axis", C.c_int), ("dft_index", C.c_int),
                 ("dft_every", C.c_int), ("nfreq", C.c_int), ("omega", C.POINTER(C.c_double))]
 
@@ -137,6 +138,7 @@ def declare(lib) -> None:
     _proto(lib, "lx_batch_step_async", C.c_int, C.c_void_p, C.c_int)
     _proto(lib, "lx_batch_wait", C.c_int, C.c_void_p)
     srv, ll = C.c_void_p, C.c_longlong
+    _proto(lib, "lx_params_field_shape", C.c_int, P(Params), C.c_int, P(C.c_int))
     _proto(lib, "lx_server_config_init", None, P(ServerConfig))
     _proto(lib, "lx_request_init", None, P(Request))
     _proto(lib, "lx_server_create", C.c_int, P(ServerConfig), P(C.c_void_p))

@@ -590,6 +590,17 @@ extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
   return LX_OK;
 }
 
+extern "C" LX_API lx_status lx_params_field_shape(const lx_params* p, int comp, int shape[3]) {
+  if (!p || !shape || comp < 0 || comp > LX_ETOTAL) return fail(nullptr, LX_ERR_INVALID, "bad argument");
+  std::string why;
+  lx_status st = validate(p, why);
+  if (st) return fail(nullptr, st, why);
+  lx_sim tmp;
+  setup_host(&tmp, p);
+  for (int a = 0; a < 3; a++) shape[a] = tmp.ext[comp][a];
+  return LX_OK;
+}
+
 extern "C" LX_API lx_status lx_params_device_bytes(const lx_params* p, size_t* bytes) {
   if (!p || !bytes) return fail(nullptr, LX_ERR_INVALID, "null argument");
   std::string why;

@@ -20,12 +20,18 @@
 #include <cstddef>
 #include <cstdint>
 
+#ifndef LX_MARCH3
+#define LX_MARCH3 4
+#endif
+
 namespace lx {
 
 constexpr int kMaxProbes = 64;
 constexpr int kMaxDftFreq = 256;
-// Cells each thread of an update kernel walks through along x (3-D planes; planar: rows 8 apart).
+// Cells each thread of a batched update kernel walks through along x: planar rows 8 apart,
+// and 3-D planes.
 constexpr int kMarch = 4;
+constexpr int kMarch3 = LX_MARCH3;
 
 // Packed CPML slab along one axis.
 struct Slab {

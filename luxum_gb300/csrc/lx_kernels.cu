@@ -682,7 +682,7 @@ __global__ void batch_tiles_kernel(const StepParams<T, C>* __restrict__ ps, cons
       tiles[t] = make_int4(m, (lt / nkb) * 8 * kMarch, 0, (lt % nkb) * 32);
     } else {
       const int njb = (p.Ny + 7) / 8;
-      tiles[t] = make_int4(m, (lt / (nkb * njb)) * kMarch, ((lt / nkb) % njb) * 8, (lt % nkb) * 32);
+      tiles[t] = make_int4(m, (lt / (nkb * njb)) * kMarch3, ((lt / nkb) % njb) * 8, (lt % nkb) * 32);
     }
   }
 }
@@ -695,15 +695,15 @@ __global__ void block_map_kernel(const int* __restrict__ first, int n, int nbloc
   }
 }
 
-// 3-D members: a block is 32 z x 8 y cells over kMarch consecutive x planes.
+// 3-D members: a block is 32 z x 8 y cells over kMarch3 consecutive x planes.
 template <class T, class C, bool UNI>
 __global__ void __launch_bounds__(256) h_batch_3d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x, j = tl.z + threadIdx.y, i0 = tl.y;
   if (k >= p.Nz || j >= p.Ny) return;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, kMarch, tl.z, 8, tl.w, 32);
-  const int i1 = min(i0 + kMarch, p.Nx);
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, kMarch3, tl.z, 8, tl.w, 32);
+  const int i1 = min(i0 + kMarch3, p.Nx);
 #pragma unroll 1
   for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI>(p, i, j, k, tf);
 }
@@ -713,10 +713,10 @@ __global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __rest
   const int4 tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x, j = tl.z + threadIdx.y, i0 = tl.y;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, kMarch, tl.z, 8, tl.w, 32);
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, kMarch3, tl.z, 8, tl.w, 32);
   typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz && j < p.Ny) {
-    const int i1 = min(i0 + kMarch, p.Nx);
+    const int i1 = min(i0 + kMarch3, p.Nx);
 #pragma unroll 1
     for (int i = i0; i < i1; ++i) {
       const typename MaxBits<C>::type b = e_cell_3d<T, C, UNI, true>(p, i, j, k, tf);
@@ -1066,7 +1066,7 @@ cudaError_t launch_batch_step(const StepParams<T, C>* ps, const int4* tiles, int
 
 int batch_blocks(int Nx, int Ny, int Nz, bool planar) {
   if (planar) return ((Nz + 31) / 32) * ((Nx + 8 * kMarch - 1) / (8 * kMarch));
-  return ((Nz + 31) / 32) * ((Ny + 7) / 8) * ((Nx + kMarch - 1) / kMarch);
+  return ((Nz + 31) / 32) * ((Ny + 7) / 8) * ((Nx + kMarch3 - 1) / kMarch3);
 }
 
 cudaError_t launch_block_map(const int* first, int n, int nblocks, int2* map, cudaStream_t s) {

@@ -43,6 +43,8 @@ struct Request {
   long long id = 0;
   lx_params params;
   int steps = 0;
+  std::vector<double> material[3];
+  double material_scale = 1.0;
   std::vector<int> boxes;
   std::vector<double> box_eps;
   int dft_axis = 0, dft_index = 0, dft_every = 1;
@@ -115,6 +117,9 @@ lx_status make_sim(Request& r) {
     r.err = lx_last_error(nullptr);
     return st;
   }
+  for (int c = 0; c < 3 && !st; c++)
+    if (!r.material[c].empty())
+      st = lx_sim_set_material(s, c, r.material[c].data(), r.material[c].size(), r.material_scale);
   for (size_t b = 0; b < r.box_eps.size() && !st; b++)
     st = lx_sim_set_eps_box(s, &r.boxes[6 * b], &r.boxes[6 * b + 3], r.box_eps[b]);
   if (!st && !r.omega.empty())
@@ -299,6 +304,7 @@ extern "C" LX_API void lx_request_init(lx_request* r) {
   if (!r) return;
   std::memset(r, 0, sizeof *r);
   lx_params_init(&r->params);
+  r->material_scale = 1.0;
   r->dft_every = 1;
 }
 
@@ -361,6 +367,15 @@ extern "C" LX_API lx_status lx_server_submit(lx_server* srv, const lx_request* r
   auto r = std::make_shared<Request>();
   r->params = req->params;
   r->steps = req->steps;
+  for (int c = 0; c < 3; c++) {
+    if (!req->material[c]) continue;
+    int shp[3];
+    if ((st = lx_params_field_shape(&req->params, c, shp))) return st;
+    const size_t n = (size_t)shp[0] * shp[1] * shp[2];
+    if (n == 0) return sfail(LX_ERR_INVALID, "material given for a component this grid does not have");
+    r->material[c].assign(req->material[c], req->material[c] + n);
+  }
+  r->material_scale = req->material_scale;
   r->boxes.assign(req->boxes, req->boxes + 6 * (size_t)req->n_boxes);
   r->box_eps.assign(req->box_eps, req->box_eps + req->n_boxes);
   r->dft_axis = req->dft_axis;
@@ -372,6 +387,7 @@ extern "C" LX_API lx_status lx_server_submit(lx_server* srv, const lx_request* r
   // DFT accumulators: nfreq x 4 components x plane x (re, im)
   const double plane = req->dft_axis == 0 ? Ny * Nz : (req->dft_axis == 1 ? Nx * Nz : Nx * Ny);
   r->bytes = (double)bytes + 64.0 * req->nfreq * plane;
+  for (int c = 0; c < 3; c++) r->bytes += 8.0 * r->material[c].size();  // transfer staging
   std::lock_guard<std::mutex> lk(srv->mu);
   r->id = srv->next_id++;
   r->t_submit = srv->now();

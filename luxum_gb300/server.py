@@ -35,14 +35,22 @@ class Server:
         if st:
             raise LuxumError(st, self.lib.lx_last_error(None).decode())
 
-    def submit(self, p: Params | dict, steps: int, boxes: Sequence = (), dft: tuple | None = None) -> int:
-        """boxes: [(lo, hi, eps_r), ...]; dft: (axis, index, omega array, every)."""
+    def submit(self, p: Params | dict, steps: int, boxes: Sequence = (), dft: tuple | None = None,
+               material: dict | None = None, material_scale: float = 1.0) -> int:
+        """boxes: [(lo, hi, eps_r), ...]; dft: (axis, index, omega array, every);
+        material: {E component: F array of its staggered extent} (Cb = dt/(eps0*(1+F*scale)))."""
         if isinstance(p, dict):
             p = params(**p)
         r = Request()
         self.lib.lx_request_init(C.byref(r))
         r.params = p
         r.steps = steps
+        keep = []
+        for c, F in (material or {}).items():
+            a = np.ascontiguousarray(F, dtype=np.float64)
+            keep.append(a)
+            r.material[c] = a.ctypes.data_as(C.POINTER(C.c_double))
+        r.material_scale = material_scale
         b = np.array([list(lo) + list(hi) for lo, hi, _ in boxes], dtype=np.int32).reshape(-1)
         e = np.array([eps for _, _, eps in boxes], dtype=np.float64)
         r.n_boxes = len(boxes)

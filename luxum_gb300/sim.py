@@ -37,6 +37,15 @@ def device_bytes(p: Params) -> int:
     return n.value
 
 
+def field_shape(p: Params, comp: int) -> tuple:
+    """Staggered extent of a component for parameters p (host only)."""
+    shp = (C.c_int * 3)()
+    st = _ffi.lib().lx_params_field_shape(C.byref(p), comp, shp)
+    if st:
+        raise LuxumError(st, _ffi.lib().lx_last_error(None).decode())
+    return (shp[0], shp[1], shp[2])
+
+
 def read_yaml(path: str) -> Params:
     """Parses a Luxum parameters.yaml (reader::readYAML + checkData)."""
     p = Params()

@@ -120,3 +120,32 @@ def test_yaml_errors(engine, tmp_path, mutation, status):
     with pytest.raises(LuxumError) as ei:
         read_yaml(bad)
     assert ei.value.status == status
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Sizes and member offsets of the ABI structs as a C compiler lays them out."""
+    import shutil
+    import subprocess
+
+    from luxum_gb300 import _ffi
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    structs = {"lx_params": _ffi.Params, "lx_request": _ffi.Request, "lx_server_config": _ffi.ServerConfig,
+               "lx_server_stats": _ffi.ServerStats, "lx_info": _ffi.Info}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "luxum.h"', "int main(void) {"]
+    for name, py in structs.items():
+        lines.append(f'  printf("{name} %zu\\n", sizeof({name}));')
+        for field, _ in py._fields_:
+            lines.append(f'  printf("{name}.{field} %zu\\n", offsetof({name}, {field}));')
+    lines.append("  return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    for name, py in structs.items():
+        assert int(got[name]) == C.sizeof(py), name
+        for field, _ in py._fields_:
+            assert int(got[f"{name}.{field}"]) == getattr(py, field).offset, (name, field)

@@ -122,3 +122,29 @@ def test_server_rejects_bad_requests(engine):
         q.Nx = 2
         with pytest.raises(LuxumError):
             srv.submit(q, 10)  # reader::checkData-style rejection
+
+
+def test_server_material_arrays(engine):
+    """Requests carrying material arrays (the batch workload's lens maps) equal solo runs."""
+    from luxum_gb300 import Server, Sim, field_shape
+
+    rng = np.random.default_rng(9)
+    planar, three = _params("planar_pml_axis"), _params("3d_pml_axis")
+    Fp = {1: (rng.random(field_shape(planar, 1)) < 0.3) * 1.5}
+    F3 = {c: (rng.random(field_shape(three, c)) < 0.2) * 3e-6 for c in range(3)}
+    with Server(chunk=20) as srv:
+        a = srv.submit(planar, 90, material=Fp, material_scale=1.0)
+        b = srv.submit(three, 50, boxes=[((12, 10, 12), (18, 16, 20), 6.0)], material=F3, material_scale=1e6)
+        assert srv.wait(a, 120.0) == "done" and srv.wait(b, 120.0) == "done"
+        ga, gb = srv.take(a, planar), srv.take(b, three)
+    sa, sb = Sim(planar), Sim(three)
+    sa.set_material(1, Fp[1], 1.0)
+    for c in range(3):
+        sb.set_material(c, F3[c], 1e6)
+    sb.set_eps_box((12, 10, 12), (18, 16, 20), 6.0)
+    sa.step(90)
+    sb.step(50)
+    for g, s in ((ga, sa), (gb, sb)):
+        for c in range(6):
+            if np.prod(s.shape(c)):
+                assert np.array_equal(g.field(c), s.field(c)), c
