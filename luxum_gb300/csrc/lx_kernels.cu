@@ -80,6 +80,23 @@ __device__ __forceinline__ bool tile_meets_planes(const int (&pl)[3][2], int i0,
   return t;
 }
 
+// Whether a tile [i0,i0+ni) x [j0,j0+nj) x [k0,k0+nk) lies where every component of both
+// half steps updates (every index in [1, N-2]) and no CPML slab reaches.  Such tiles (most
+// of a grid) take the cell code with every per-cell condition decided at compile time.
+__device__ __forceinline__ bool axis_free(const Slab& s, int a, int n) { return s.n == 0 || (a >= s.lo && a + n <= s.hi0); }
+__device__ __forceinline__ bool tile_is_interior(const Slab (&sl)[3], bool pml, int Nx, int Ny, int Nz, int i0, int ni,
+                                                 int j0, int nj, int k0, int nk) {
+  if (i0 < 1 || i0 + ni > Nx - 1 || j0 < 1 || j0 + nj > Ny - 1 || k0 < 1 || k0 + nk > Nz - 1) return false;
+  return !pml || (axis_free(sl[0], i0, ni) && axis_free(sl[1], j0, nj) && axis_free(sl[2], k0, nk));
+}
+
+// The same for a planar tile [i0,i0+ni) x [k0,k0+nk) (no y axis).
+__device__ __forceinline__ bool tile_is_interior_2d(const Slab (&sl)[3], bool pml, int Nx, int Nz, int i0, int ni,
+                                                    int k0, int nk) {
+  if (i0 < 1 || i0 + ni > Nx - 1 || k0 < 1 || k0 + nk > Nz - 1) return false;
+  return !pml || (axis_free(sl[0], i0, ni) && axis_free(sl[2], k0, nk));
+}
+
 // psi = b*psi + c*curl; returns curl/kappa + psi (reference: three_dim_pml.cc:186-188).
 template <class C>
 __device__ __forceinline__ C pml_term(C d, C* psi, C b, C cc, C rk) {
@@ -251,10 +268,11 @@ struct HCell {
   C ex, ey, ez, ez_j, ey_k, ex_k, ez_i, ey_i, ex_j, hx, hy, hz;
 };
 
-template <class T, class C>
+template <class T, class C, bool FAST = false>
 __device__ __forceinline__ void h_load(const StepParams<T, C>& p, const int i, const int j, const int k, HCell<C>& v) {
   const long long c = (long long)i * p.si + (long long)j * p.sj + k;
-  const bool ux = (j < p.Ny - 1 && k < p.Nz - 1), uy = (i < p.Nx - 1 && k < p.Nz - 1), uz = (i < p.Nx - 1 && j < p.Ny - 1);
+  const bool ux = FAST || (j < p.Ny - 1 && k < p.Nz - 1), uy = FAST || (i < p.Nx - 1 && k < p.Nz - 1),
+             uz = FAST || (i < p.Nx - 1 && j < p.Ny - 1);
   v.c = c;
   v.ux = ux;
   v.uy = uy;
@@ -275,15 +293,16 @@ __device__ __forceinline__ void h_load(const StepParams<T, C>& p, const int i, c
   v.hz = uz ? ld<T, C>(p.H[2] + c) : C(0);
 }
 
-template <class T, class C, bool UNI>
-__device__ __forceinline__ void h_apply(const StepParams<T, C>& p, const int i, const int j, const int k, const bool tf,
+template <class T, class C, bool UNI, bool FAST = false>
+__device__ __forceinline__ void h_apply(const StepParams<T, C>& p, const int i, const int j, const int k, bool tf,
                                         const HCell<C>& v) {
   const long long c = v.c;
-  const bool ux = v.ux, uy = v.uy, uz = v.uz;
+  const bool ux = FAST || v.ux, uy = FAST || v.uy, uz = FAST || v.uz;
+  if (FAST) tf = false;
   const C ex = v.ex, ey = v.ey, ez = v.ez, ez_j = v.ez_j, ey_k = v.ey_k, ex_k = v.ex_k, ez_i = v.ez_i, ey_i = v.ey_i,
           ex_j = v.ex_j, hx = v.hx, hy = v.hy, hz = v.hz;
   int sx = -1, sy = -1, sz = -1;
-  if (p.pml) {
+  if (!FAST && p.pml) {
     sx = slab_index(p.slab[0], i);
     sy = slab_index(p.slab[1], j);
     sz = slab_index(p.slab[2], k);
@@ -330,12 +349,12 @@ __device__ __forceinline__ void h_apply(const StepParams<T, C>& p, const int i, 
   if (uz) st<T, C>(p.H[2] + c, nhz);
 }
 
-template <class T, class C, bool UNI>
+template <class T, class C, bool UNI, bool FAST = false>
 __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i, const int j, const int k,
                                           const bool tf) {
   HCell<C> v;
-  h_load<T, C>(p, i, j, k, v);
-  h_apply<T, C, UNI>(p, i, j, k, tf, v);
+  h_load<T, C, FAST>(p, i, j, k, v);
+  h_apply<T, C, UNI, FAST>(p, i, j, k, tf, v);
 }
 
 // Each block owns a 32 (z) x 8 (y) column of cells over kMarch consecutive x planes; each
@@ -357,7 +376,10 @@ __global__ void __launch_bounds__(256, HMinBlocks<C>::v) h_kernel_3d(const StepP
   if (k >= p.Nz || j >= p.Ny) return;
   const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, M, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
   if constexpr (M == 1) {
-    h_cell_3d<T, C, UNI>(p, i0, j, k, tf);
+    if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i0, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32))
+      h_cell_3d<T, C, UNI, true>(p, i0, j, k, false);
+    else
+      h_cell_3d<T, C, UNI>(p, i0, j, k, tf);
   } else {
     const int i1 = min(i0 + M, p.Nx);
 #pragma unroll 1
@@ -376,12 +398,13 @@ struct ECell {
   C hx, hy, hz, hz_j, hy_k, hx_k, hz_i, hy_i, hx_j, ex, ey, ez, cbx, cby, cbz;
 };
 
-template <class T, class C, bool MON>
+template <class T, class C, bool MON, bool FAST = false>
 __device__ __forceinline__ void e_load(const StepParams<T, C>& p, const int i, const int j, const int k, ECell<C>& v) {
   const long long c = (long long)i * p.si + (long long)j * p.sj + k;
   const bool ii = (i >= 1 && i < p.Nx - 1), jj = (j >= 1 && j < p.Ny - 1), kk = (k >= 1 && k < p.Nz - 1);
-  const bool ux = (i < p.Nx - 1 && jj && kk), uy = (ii && j < p.Ny - 1 && kk), uz = (ii && jj && k < p.Nz - 1);
-  const bool mon = MON && i < p.Nx - 1 && j < p.Ny - 1 && k < p.Nz - 1;
+  const bool ux = FAST || (i < p.Nx - 1 && jj && kk), uy = FAST || (ii && j < p.Ny - 1 && kk),
+             uz = FAST || (ii && jj && k < p.Nz - 1);
+  const bool mon = MON && (FAST || (i < p.Nx - 1 && j < p.Ny - 1 && k < p.Nz - 1));
   v.c = c;
   v.ux = ux;
   v.uy = uy;
@@ -405,15 +428,16 @@ __device__ __forceinline__ void e_load(const StepParams<T, C>& p, const int i, c
   v.cbz = uz ? p.Cbs[2][c] : C(0);
 }
 
-template <class T, class C, bool UNI, bool MON>
+template <class T, class C, bool UNI, bool MON, bool FAST = false>
 __device__ __forceinline__ typename MaxBits<C>::type e_apply(const StepParams<T, C>& p, const int i, const int j,
-                                                             const int k, const bool tf, const ECell<C>& v) {
+                                                             const int k, bool tf, const ECell<C>& v) {
   const long long c = v.c;
-  const bool ux = v.ux, uy = v.uy, uz = v.uz, mon = v.mon;
+  const bool ux = FAST || v.ux, uy = FAST || v.uy, uz = FAST || v.uz, mon = MON && (FAST || v.mon);
+  if (FAST) tf = false;
   const C hx = v.hx, hy = v.hy, hz = v.hz, hz_j = v.hz_j, hy_k = v.hy_k, hx_k = v.hx_k, hz_i = v.hz_i, hy_i = v.hy_i,
           hx_j = v.hx_j, ex = v.ex, ey = v.ey, ez = v.ez, cbx = v.cbx, cby = v.cby, cbz = v.cbz;
   int sx = -1, sy = -1, sz = -1;
-  if (p.pml) {
+  if (!FAST && p.pml) {
     sx = slab_index(p.slab[0], i);
     sy = slab_index(p.slab[1], j);
     sz = slab_index(p.slab[2], k);
@@ -468,12 +492,12 @@ __device__ __forceinline__ typename MaxBits<C>::type e_apply(const StepParams<T,
   return mbits;
 }
 
-template <class T, class C, bool UNI, bool MON>
+template <class T, class C, bool UNI, bool MON, bool FAST = false>
 __device__ __forceinline__ typename MaxBits<C>::type e_cell_3d(const StepParams<T, C>& p, const int i, const int j,
                                                                const int k, const bool tf) {
   ECell<C> v;
-  e_load<T, C, MON>(p, i, j, k, v);
-  return e_apply<T, C, UNI, MON>(p, i, j, k, tf, v);
+  e_load<T, C, MON, FAST>(p, i, j, k, v);
+  return e_apply<T, C, UNI, MON, FAST>(p, i, j, k, tf, v);
 }
 
 template <class T, class C, bool UNI, bool MON, int M>
@@ -485,6 +509,7 @@ __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
   typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz && j < p.Ny) {
     if constexpr (M == 1) {
+      // (the interior fast path gains nothing here and costs FP16 storage 9 %)
       mbits = e_cell_3d<T, C, UNI, MON>(p, i0, j, k, tf);
     } else {
       const int i1 = min(i0 + M, p.Nx);
@@ -509,10 +534,10 @@ struct HCell2 {
   C ey, ey_k, ey_i, hx, hz;
 };
 
-template <class T, class C>
+template <class T, class C, bool FAST = false>
 __device__ __forceinline__ void h2_load(const StepParams<T, C>& p, const int i, const int k, HCell2<C>& v) {
   const long long c = (long long)i * p.si + k;
-  const bool ux = k < p.Nz - 1, uz = i < p.Nx - 1;
+  const bool ux = FAST || k < p.Nz - 1, uz = FAST || i < p.Nx - 1;
   v.c = c;
   v.ux = ux;
   v.uz = uz;
@@ -523,11 +548,12 @@ __device__ __forceinline__ void h2_load(const StepParams<T, C>& p, const int i, 
   v.hz = uz ? ld<T, C>(p.H[2] + c) : C(0);
 }
 
-template <class T, class C, bool UNI>
-__device__ __forceinline__ void h2_apply(const StepParams<T, C>& p, const int i, const int k, const bool tf,
+template <class T, class C, bool UNI, bool FAST = false>
+__device__ __forceinline__ void h2_apply(const StepParams<T, C>& p, const int i, const int k, bool tf,
                                          const HCell2<C>& v) {
   const long long c = v.c;
-  const bool ux = v.ux, uz = v.uz;
+  const bool ux = FAST || v.ux, uz = FAST || v.uz;
+  if (FAST) tf = false;
   const C ey = v.ey, ey_k = v.ey_k, ey_i = v.ey_i, hx = v.hx, hz = v.hz;
   C nhx = hx, nhz = hz;
   // Hx: k < Nz-1; Hx -= Db*(-curl2/kappa - psi2), curl2 = dEy/dz (z profile)
@@ -535,7 +561,7 @@ __device__ __forceinline__ void h2_apply(const StepParams<T, C>& p, const int i,
     C d2 = ey_k - ey;
     if (!UNI) d2 *= p.rd[2];
     if (tf) tfsf_apply<C>(p.setsH[0][1], p.tab, i, 0, k, d2);
-    if (p.pml) {
+    if (!FAST && p.pml) {
       const int sz = slab_index(p.slab[2], k);
       if (sz >= 0) d2 = pml_term<C>(d2, p.psiH[0][1] + (long long)i * p.slab[2].n + sz, p.bH[2][k], p.cH[2][k], p.rkH[2][k]);
     }
@@ -546,7 +572,7 @@ __device__ __forceinline__ void h2_apply(const StepParams<T, C>& p, const int i,
     C d1 = ey_i - ey;
     if (!UNI) d1 *= p.rd[0];
     if (tf) tfsf_apply<C>(p.setsH[2][0], p.tab, i, 0, k, d1);
-    if (p.pml) {
+    if (!FAST && p.pml) {
       const int sx = slab_index(p.slab[0], i);
       if (sx >= 0) d1 = pml_term<C>(d1, p.psiH[2][0] + (long long)sx * p.Nzp + k, p.bH[0][i], p.cH[0][i], p.rkH[0][i]);
     }
@@ -556,11 +582,11 @@ __device__ __forceinline__ void h2_apply(const StepParams<T, C>& p, const int i,
   if (uz) st<T, C>(p.H[2] + c, nhz);
 }
 
-template <class T, class C, bool UNI>
+template <class T, class C, bool UNI, bool FAST = false>
 __device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i, const int k, const bool tf) {
   HCell2<C> v;
-  h2_load<T, C>(p, i, k, v);
-  h2_apply<T, C, UNI>(p, i, k, tf, v);
+  h2_load<T, C, FAST>(p, i, k, v);
+  h2_apply<T, C, UNI, FAST>(p, i, k, tf, v);
 }
 
 // Each block owns 32 (z) x 8*kMarch (x) cells; thread row r handles x rows r, r+8, ...
@@ -570,10 +596,12 @@ __global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
   const int ib = blockIdx.y * 8 * M;
   if (k >= p.Nz) return;
   const bool tf = p.tfsf && tile_meets_planes(p.planesH, ib, 8 * M, 0, 1, blockIdx.x * 32, 32);
+  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, ib, 8 * M, blockIdx.x * 32, 32);
 #pragma unroll 1
   for (int r = 0; r < M; ++r) {
     const int i = ib + threadIdx.y + 8 * r;
-    if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
+    if (fast) h_cell_2d<T, C, UNI, true>(p, i, k, false);
+    else if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
   }
 }
 
@@ -587,10 +615,10 @@ struct ECell2 {
   C ey, hx, hx_k, hz, hz_i, cb;
 };
 
-template <class T, class C, bool MON>
+template <class T, class C, bool MON, bool FAST = false>
 __device__ __forceinline__ void e2_load(const StepParams<T, C>& p, const int i, const int k, ECell2<C>& v) {
   const long long c = (long long)i * p.si + k;
-  const bool u = (i >= 1 && i < p.Nx - 1 && k >= 1 && k < p.Nz - 1);
+  const bool u = FAST || (i >= 1 && i < p.Nx - 1 && k >= 1 && k < p.Nz - 1);
   v.c = c;
   v.u = u;
   v.ey = (u || MON) ? ld<T, C>(p.E[1] + c) : C(0);
@@ -601,13 +629,14 @@ __device__ __forceinline__ void e2_load(const StepParams<T, C>& p, const int i, 
   v.cb = u ? p.Cbs[1][c] : C(0);
 }
 
-template <class T, class C, bool UNI, bool MON>
+template <class T, class C, bool UNI, bool MON, bool FAST = false>
 __device__ __forceinline__ typename MaxBits<C>::type e2_apply(const StepParams<T, C>& p, const int i, const int k,
-                                                              const bool tf, const ECell2<C>& v) {
+                                                              bool tf, const ECell2<C>& v) {
   const long long c = v.c;
   const C ey = v.ey;
   C eyn = ey;
-  if (v.u) {
+  if (FAST) tf = false;
+  if (FAST || v.u) {
     C d1 = v.hx - v.hx_k;  // dHx/dz (z profile)
     C d2 = v.hz - v.hz_i;  // dHz/dx (x profile)
     if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
@@ -615,7 +644,7 @@ __device__ __forceinline__ typename MaxBits<C>::type e2_apply(const StepParams<T
       tfsf_apply<C>(p.setsE[1][0], p.tab, i, 0, k, d1);
       tfsf_apply<C>(p.setsE[1][1], p.tab, i, 0, k, d2);
     }
-    if (p.pml) {
+    if (!FAST && p.pml) {
       const int sz = slab_index(p.slab[2], k), sx = slab_index(p.slab[0], i);
       if (sz >= 0) d1 = pml_term<C>(d1, p.psiE[1][0] + (long long)i * p.slab[2].n + sz, p.bE[2][k], p.cE[2][k], p.rkE[2][k]);
       if (sx >= 0) d2 = pml_term<C>(d2, p.psiE[1][1] + (long long)sx * p.Nzp + k, p.bE[0][i], p.cE[0][i], p.rkE[0][i]);
@@ -627,12 +656,12 @@ __device__ __forceinline__ typename MaxBits<C>::type e2_apply(const StepParams<T
   return MON ? MaxBits<C>::of(eyn * eyn) : typename MaxBits<C>::type(0);
 }
 
-template <class T, class C, bool UNI, bool MON>
+template <class T, class C, bool UNI, bool MON, bool FAST = false>
 __device__ __forceinline__ typename MaxBits<C>::type e_cell_2d(const StepParams<T, C>& p, const int i, const int k,
                                                                const bool tf) {
   ECell2<C> v;
-  e2_load<T, C, MON>(p, i, k, v);
-  return e2_apply<T, C, UNI, MON>(p, i, k, tf, v);
+  e2_load<T, C, MON, FAST>(p, i, k, v);
+  return e2_apply<T, C, UNI, MON, FAST>(p, i, k, tf, v);
 }
 
 template <class T, class C, bool UNI, bool MON, int M>
@@ -640,15 +669,16 @@ __global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int ib = blockIdx.y * 8 * M;
   const bool tf = p.tfsf && tile_meets_planes(p.planesE, ib, 8 * M, 0, 1, blockIdx.x * 32, 32);
+  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, ib, 8 * M, blockIdx.x * 32, 32);
   typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz) {
 #pragma unroll 1
     for (int r = 0; r < M; ++r) {
       const int i = ib + threadIdx.y + 8 * r;
-      if (i < p.Nx) {
-        const typename MaxBits<C>::type b = e_cell_2d<T, C, UNI, MON>(p, i, k, tf);
-        mbits = b > mbits ? b : mbits;
-      }
+      typename MaxBits<C>::type b = 0;
+      if (fast) b = e_cell_2d<T, C, UNI, MON, true>(p, i, k, false);
+      else if (i < p.Nx) b = e_cell_2d<T, C, UNI, MON>(p, i, k, tf);
+      mbits = b > mbits ? b : mbits;
     }
   }
   if (MON && p.max_slot) block_max_atomic(mbits, p.max_slot);
@@ -704,8 +734,13 @@ __global__ void __launch_bounds__(256) h_batch_3d(const StepParams<T, C>* __rest
   if (k >= p.Nz || j >= p.Ny) return;
   const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, kMarch3, tl.z, 8, tl.w, 32);
   const int i1 = min(i0 + kMarch3, p.Nx);
+  if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i0, kMarch3, tl.z, 8, tl.w, 32)) {
 #pragma unroll 1
-  for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI>(p, i, j, k, tf);
+    for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI, true>(p, i, j, k, false);
+  } else {
+#pragma unroll 1
+    for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI>(p, i, j, k, tf);
+  }
 }
 
 template <class T, class C, bool UNI>
@@ -717,10 +752,18 @@ __global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __rest
   typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz && j < p.Ny) {
     const int i1 = min(i0 + kMarch3, p.Nx);
+    if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i0, kMarch3, tl.z, 8, tl.w, 32)) {
 #pragma unroll 1
-    for (int i = i0; i < i1; ++i) {
-      const typename MaxBits<C>::type b = e_cell_3d<T, C, UNI, true>(p, i, j, k, tf);
-      mbits = b > mbits ? b : mbits;
+      for (int i = i0; i < i1; ++i) {
+        const typename MaxBits<C>::type b = e_cell_3d<T, C, UNI, true, true>(p, i, j, k, false);
+        mbits = b > mbits ? b : mbits;
+      }
+    } else {
+#pragma unroll 1
+      for (int i = i0; i < i1; ++i) {
+        const typename MaxBits<C>::type b = e_cell_3d<T, C, UNI, true>(p, i, j, k, tf);
+        mbits = b > mbits ? b : mbits;
+      }
     }
   }
   if (p.max_slot) block_max_atomic(mbits, p.max_slot);
@@ -736,10 +779,12 @@ __global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __rest
   const int k = tl.w + threadIdx.x;
   if (k >= p.Nz) return;
   const bool tf = p.tfsf && tile_meets_planes(p.planesH, tl.y, 8 * kMarch, 0, 1, tl.w, 32);
+  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, tl.y, 8 * kMarch, tl.w, 32);
 #pragma unroll 1
   for (int r = 0; r < kMarch; ++r) {
     const int i = tl.y + threadIdx.y + 8 * r;
-    if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
+    if (fast) h_cell_2d<T, C, UNI, true>(p, i, k, false);
+    else if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
   }
 }
 
@@ -749,15 +794,16 @@ __global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __rest
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x;
   const bool tf = p.tfsf && tile_meets_planes(p.planesE, tl.y, 8 * kMarch, 0, 1, tl.w, 32);
+  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, tl.y, 8 * kMarch, tl.w, 32);
   typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz) {
 #pragma unroll 1
     for (int r = 0; r < kMarch; ++r) {
       const int i = tl.y + threadIdx.y + 8 * r;
-      if (i < p.Nx) {
-        const typename MaxBits<C>::type b = e_cell_2d<T, C, UNI, true>(p, i, k, tf);
-        mbits = b > mbits ? b : mbits;
-      }
+      typename MaxBits<C>::type b = 0;
+      if (fast) b = e_cell_2d<T, C, UNI, true, true>(p, i, k, false);
+      else if (i < p.Nx) b = e_cell_2d<T, C, UNI, true>(p, i, k, tf);
+      mbits = b > mbits ? b : mbits;
     }
   }
   if (p.max_slot) block_max_atomic(mbits, p.max_slot);
