@@ -248,6 +248,9 @@ def bench_batch(args):
     batch = Batch(chunk=100)
     for s in sims:
         batch.add(s)
+    t_tune = time.perf_counter()
+    march = batch.autotune(20)  # tile shape timed on twins of the members, outside the timed region
+    t_tune = time.perf_counter() - t_tune
 
     def run():
         for s in sims:
@@ -283,7 +286,9 @@ def bench_batch(args):
             "s_per_run": dt / args.steps, "dtype": "f32",
             "unbatched_sample": {"sims": len(sample), "value": solo, "steps": args.solo_steps,
                                  "note": "same simulations stepped one handle at a time with lx_sim_step"},
-            "batched_over_unbatched": value / solo, "clocks": clk.summary()}
+            "batched_over_unbatched": value / solo, "autotuned_march": {"planar_rows": march[0], "planes_3d": march[1],
+                                                                       "seconds": t_tune},
+            "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     batch.close()
 

@@ -273,6 +273,15 @@ LX_API lx_status lx_batch_step(lx_batch* b, int nsteps);
  * read-back, blow-up check).  Members must not be touched in between. */
 LX_API lx_status lx_batch_step_async(lx_batch* b, int nsteps);
 LX_API lx_status lx_batch_wait(lx_batch* b);
+/* Tile shape of the batched update kernels: cells each thread walks along x, for planar
+ * members (rows 8 apart) and for 3-D members (planes); each 1, 2, 4 or 8 (defaults 8, 4).
+ * Results do not depend on it, only speed. */
+LX_API lx_status lx_batch_set_march(lx_batch* b, int planar_rows, int planes_3d);
+LX_API lx_status lx_batch_get_march(const lx_batch* b, int* planar_rows, int* planes_3d);
+/* Picks the march per dimension by timing `steps` batched steps of each candidate on
+ * zero-field twins of a sample of the members (up to 1.5e8 cells per dimension, created
+ * and freed here); the members themselves are not stepped.  Reports the choice. */
+LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* planar_rows, int* planes_3d);
 
 /* ---- Serving: continuous batching of submitted simulations --------------------------
  * No reference counterpart: the reference runs one simulation per process.  A server owns

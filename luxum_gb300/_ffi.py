@@ -137,6 +137,9 @@ def declare(lib) -> None:
     _proto(lib, "lx_batch_step", C.c_int, C.c_void_p, C.c_int)
     _proto(lib, "lx_batch_step_async", C.c_int, C.c_void_p, C.c_int)
     _proto(lib, "lx_batch_wait", C.c_int, C.c_void_p)
+    _proto(lib, "lx_batch_set_march", C.c_int, C.c_void_p, C.c_int, C.c_int)
+    _proto(lib, "lx_batch_get_march", C.c_int, C.c_void_p, P(C.c_int), P(C.c_int))
+    _proto(lib, "lx_batch_autotune", C.c_int, C.c_void_p, C.c_int, P(C.c_int), P(C.c_int))
     srv, ll = C.c_void_p, C.c_longlong
     _proto(lib, "lx_params_field_shape", C.c_int, P(Params), C.c_int, P(C.c_int))
     _proto(lib, "lx_server_config_init", None, P(ServerConfig))

@@ -1588,12 +1588,14 @@ struct lx_batch {
   cudaStream_t stream = nullptr;
   struct Group {  // members sharing (planar, uniform): one update launch per half step
     bool planar = false, uniform = false;
+    int march = lx::kMarch3;   // cells each thread walks along x
     std::vector<int> members;  // batch-global indices
     void* d_params = nullptr;
     int* d_first = nullptr;
     int4* d_tiles = nullptr;
     int nblocks = 0;
   };
+  int march2d = lx::kMarch2, march3d = lx::kMarch3;  // per dimension (lx_batch_set_march / autotune)
   struct DftClass {  // DFT planes that sample at the same batch steps
     int every = 1, phase = 0;
     lx::DftParams* d_planes = nullptr;
@@ -1770,6 +1772,7 @@ static lx_status batch_rebuild(lx_batch* b) {
       b->groups.emplace_back();
       b->groups.back().planar = s->planar;
       b->groups.back().uniform = s->uniform;
+      b->groups.back().march = s->planar ? b->march2d : b->march3d;
       gi = (int)b->groups.size() - 1;
     }
     b->groups[gi].members.push_back(q);
@@ -1801,7 +1804,7 @@ static lx_status batch_rebuild(lx_batch* b) {
       sp.max_slot = b->d_slots + q;
       sp.etotal = nullptr;
       ps.push_back(sp);
-      const long long nb = (long long)first.back() + lx::batch_blocks(s->Nx, s->Ny, s->Nz, s->planar);
+      const long long nb = (long long)first.back() + lx::batch_blocks(s->Nx, s->Ny, s->Nz, s->planar, g.march);
       if (nb > 0x7fffffffLL) return bfail(b, LX_ERR_INVALID, "batch too large for one launch");
       first.push_back((int)nb);
     }
@@ -1812,7 +1815,7 @@ static lx_status batch_rebuild(lx_batch* b) {
     BCK(cudaMemcpyAsync(g.d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMallocAsync(&g.d_tiles, sizeof(int4) * (g.nblocks > 0 ? g.nblocks : 1), b->stream));
     BCK(lx::launch_batch_tiles<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_first, (int)g.members.size(), g.nblocks,
-                                     g.planar, g.d_tiles, b->stream));
+                                     g.planar, g.march, g.d_tiles, b->stream));
   }
   b->dirty = false;
   return LX_OK;
@@ -1825,10 +1828,10 @@ static lx_status batch_enqueue(lx_batch* b, long long step0, int nsteps) {
     BCK(lx::launch_prologue_batch<C>(b->d_pps, b->d_ts, n, b->max_entries, b->stream));
     for (auto& g : b->groups)
       BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.nblocks, g.planar,
-                                      g.uniform, true, b->stream));
+                                      g.uniform, g.march, true, b->stream));
     for (auto& g : b->groups)
       BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.nblocks, g.planar,
-                                      g.uniform, false, b->stream));
+                                      g.uniform, g.march, false, b->stream));
     const long long bs = step0 + q;
     for (auto& cl : b->dft)
       if (bs % cl.every == cl.phase)
@@ -1915,4 +1918,99 @@ extern "C" LX_API lx_status lx_batch_step(lx_batch* b, int nsteps) {
   lx_status st = lx_batch_step_async(b, nsteps);
   if (st) return st;
   return lx_batch_wait(b);
+}
+
+static bool march_ok(int m) { return m == 1 || m == 2 || m == 4 || m == 8; }
+
+extern "C" LX_API lx_status lx_batch_set_march(lx_batch* b, int planar_rows, int planes_3d) {
+  if (!b || !march_ok(planar_rows) || !march_ok(planes_3d)) return fail(nullptr, LX_ERR_INVALID, "march must be 1, 2, 4 or 8");
+  lx_status st = lx_batch_wait(b);
+  if (st) return st;
+  b->march2d = planar_rows;
+  b->march3d = planes_3d;
+  b->dirty = true;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  b->exec_steps = 0;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_batch_get_march(const lx_batch* b, int* planar_rows, int* planes_3d) {
+  if (!b || !planar_rows || !planes_3d) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  *planar_rows = b->march2d;
+  *planes_3d = b->march3d;
+  return LX_OK;
+}
+
+// Times `steps` batched steps of twins (zero fields, same parameters and Cb) of a sample of
+// the members of one dimension for each march length, on a scratch batch; the members
+// themselves are not touched.  Returns the fastest march, or 0 if there is nothing to time.
+static lx_status tune_dimension(lx_batch* b, bool planar, int steps, double cell_budget, int* best) {
+  *best = 0;
+  std::vector<lx_sim*> sample;
+  double cells = 0.0;
+  for (auto* s : b->sims) {
+    if ((bool)s->planar != planar) continue;
+    const double c = (double)s->Nx * s->Ny * s->Nz;
+    if (!sample.empty() && cells + c > cell_budget) continue;
+    sample.push_back(s);
+    cells += c;
+  }
+  if (sample.empty()) return LX_OK;
+  std::vector<lx_sim*> twins;
+  lx_batch* tb = nullptr;
+  lx_status st = lx_batch_create(&tb);
+  if (!st) st = lx_batch_set_chunk(tb, 0);
+  for (size_t q = 0; q < sample.size() && !st; q++) {
+    lx_sim* t = nullptr;
+    st = lx_sim_create(&sample[q]->p, &t);
+    if (st) break;
+    twins.push_back(t);
+    for (int c = 0; c < 3 && !st; c++)
+      if (sample[q]->Cbs[c] && ext_n(sample[q], c))
+        if (cudaMemcpyAsync(t->Cbs[c], sample[q]->Cbs[c], t->ncell * t->csize, cudaMemcpyDeviceToDevice, t->stream) != cudaSuccess)
+          st = fail(nullptr, LX_ERR_CUDA, "copying Cb to a tuning twin failed");
+    if (!st) st = lx_sim_sync(t);
+    if (!st) st = lx_batch_add(tb, t);
+  }
+  float best_ms = 0.f;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (!st && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+    st = fail(nullptr, LX_ERR_CUDA, "cudaEventCreate failed");
+  const int cand[4] = {1, 2, 4, 8};
+  for (int q = 0; q < 4 && !st; q++) {
+    st = lx_batch_set_march(tb, cand[q], cand[q]);
+    if (!st) st = lx_batch_step(tb, 2);  // rebuild and warm up
+    if (st) break;
+    cudaEventRecord(e0, tb->stream);
+    st = lx_batch_step_async(tb, steps);
+    cudaEventRecord(e1, tb->stream);
+    if (!st) st = lx_batch_wait(tb);
+    if (st == LX_ERR_BLOWUP) st = LX_OK;  // zero fields cannot blow up; tolerate a source-driven twin
+    float ms = 0.f;
+    if (!st && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) st = fail(nullptr, LX_ERR_CUDA, "event timing failed");
+    if (!st && (*best == 0 || ms < best_ms)) {
+      best_ms = ms;
+      *best = cand[q];
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (tb) lx_batch_destroy(tb);
+  for (auto* t : twins) lx_sim_destroy(t);
+  return st;
+}
+
+extern "C" LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* planar_rows, int* planes_3d) {
+  if (!b || steps < 1) return fail(nullptr, LX_ERR_INVALID, "steps must be >= 1");
+  lx_status st = lx_batch_wait(b);
+  if (st) return st;
+  int m2 = 0, m3 = 0;
+  const double budget = 1.5e8;  // cells of twins per dimension
+  if ((st = tune_dimension(b, true, steps, budget, &m2))) return st;
+  if ((st = tune_dimension(b, false, steps, budget, &m3))) return st;
+  if ((st = lx_batch_set_march(b, m2 ? m2 : b->march2d, m3 ? m3 : b->march3d))) return st;
+  if (planar_rows) *planar_rows = b->march2d;
+  if (planes_3d) *planes_3d = b->march3d;
+  return LX_OK;
 }

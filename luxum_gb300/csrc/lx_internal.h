@@ -20,18 +20,15 @@
 #include <cstddef>
 #include <cstdint>
 
-#ifndef LX_MARCH3
-#define LX_MARCH3 4
-#endif
-
 namespace lx {
 
 constexpr int kMaxProbes = 64;
 constexpr int kMaxDftFreq = 256;
-// Cells each thread of a batched update kernel walks through along x: planar rows 8 apart,
-// and 3-D planes.
-constexpr int kMarch = 4;
-constexpr int kMarch3 = LX_MARCH3;
+// Default cells each thread of a batched update kernel walks through along x: planar rows 8
+// apart, and 3-D planes (the autotuner's picks on the lens and serving workloads);
+// lx_batch_autotune picks per batch among 1, 2, 4 and 8.
+constexpr int kMarch2 = 8;
+constexpr int kMarch3 = 4;
 
 // Packed CPML slab along one axis.
 struct Slab {

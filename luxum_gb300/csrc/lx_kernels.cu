@@ -357,9 +357,9 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
   h_apply<T, C, UNI, FAST>(p, i, j, k, tf, v);
 }
 
-// Each block owns a 32 (z) x 8 (y) column of cells over kMarch consecutive x planes; each
+// Each block owns a 32 (z) x 8 (y) column of cells over M consecutive x planes; each
 // thread walks its column through the planes, so index set-up and the TF/SF tile test are
-// paid once per kMarch cells.
+// paid once per M cells.
 // Resident blocks per SM asked of the compiler for the H kernel (a register cap): 8 for
 // float compute (32 registers, no spills; FP16 storage 14 % faster than at 40 registers),
 // 5 for FP64 (its natural 48 registers; an explicit 1 lets the compiler take 54).
@@ -589,7 +589,7 @@ __device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i
   h2_apply<T, C, UNI, FAST>(p, i, k, tf, v);
 }
 
-// Each block owns 32 (z) x 8*kMarch (x) cells; thread row r handles x rows r, r+8, ...
+// Each block owns 32 (z) x 8*M (x) cells; thread row r handles x rows r, r+8, ...
 template <class T, class C, bool UNI, int M>
 __global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
@@ -702,17 +702,17 @@ __device__ __forceinline__ int find_member(const int* __restrict__ first, int n,
 // first x row (planar), b = first y row (3-D), c = first z cell.
 template <class T, class C>
 __global__ void batch_tiles_kernel(const StepParams<T, C>* __restrict__ ps, const int* __restrict__ first, int n,
-                                   int nblocks, int planar, int4* __restrict__ tiles) {
+                                   int nblocks, int planar, int march, int4* __restrict__ tiles) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nblocks; t += gridDim.x * blockDim.x) {
     const int m = find_member(first, n, t);
     const int lt = t - first[m];
     const StepParams<T, C>& p = ps[m];
     const int nkb = (p.Nz + 31) / 32;
     if (planar) {
-      tiles[t] = make_int4(m, (lt / nkb) * 8 * kMarch, 0, (lt % nkb) * 32);
+      tiles[t] = make_int4(m, (lt / nkb) * 8 * march, 0, (lt % nkb) * 32);
     } else {
       const int njb = (p.Ny + 7) / 8;
-      tiles[t] = make_int4(m, (lt / (nkb * njb)) * kMarch3, ((lt / nkb) % njb) * 8, (lt % nkb) * 32);
+      tiles[t] = make_int4(m, (lt / (nkb * njb)) * march, ((lt / nkb) % njb) * 8, (lt % nkb) * 32);
     }
   }
 }
@@ -725,16 +725,16 @@ __global__ void block_map_kernel(const int* __restrict__ first, int n, int nbloc
   }
 }
 
-// 3-D members: a block is 32 z x 8 y cells over kMarch3 consecutive x planes.
-template <class T, class C, bool UNI>
+// 3-D members: a block is 32 z x 8 y cells over M consecutive x planes.
+template <class T, class C, bool UNI, int M>
 __global__ void __launch_bounds__(256) h_batch_3d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x, j = tl.z + threadIdx.y, i0 = tl.y;
   if (k >= p.Nz || j >= p.Ny) return;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, kMarch3, tl.z, 8, tl.w, 32);
-  const int i1 = min(i0 + kMarch3, p.Nx);
-  if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i0, kMarch3, tl.z, 8, tl.w, 32)) {
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, M, tl.z, 8, tl.w, 32);
+  const int i1 = min(i0 + M, p.Nx);
+  if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i0, M, tl.z, 8, tl.w, 32)) {
 #pragma unroll 1
     for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI, true>(p, i, j, k, false);
   } else {
@@ -743,16 +743,16 @@ __global__ void __launch_bounds__(256) h_batch_3d(const StepParams<T, C>* __rest
   }
 }
 
-template <class T, class C, bool UNI>
+template <class T, class C, bool UNI, int M>
 __global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x, j = tl.z + threadIdx.y, i0 = tl.y;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, kMarch3, tl.z, 8, tl.w, 32);
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, M, tl.z, 8, tl.w, 32);
   typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz && j < p.Ny) {
-    const int i1 = min(i0 + kMarch3, p.Nx);
-    if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i0, kMarch3, tl.z, 8, tl.w, 32)) {
+    const int i1 = min(i0 + M, p.Nx);
+    if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i0, M, tl.z, 8, tl.w, 32)) {
 #pragma unroll 1
       for (int i = i0; i < i1; ++i) {
         const typename MaxBits<C>::type b = e_cell_3d<T, C, UNI, true, true>(p, i, j, k, false);
@@ -769,36 +769,36 @@ __global__ void __launch_bounds__(256) e_batch_3d(const StepParams<T, C>* __rest
   if (p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
-// planar members: a block is 32 z cells x 8*kMarch x rows.  Rows are walked one after the
+// planar members: a block is 32 z cells x 8*M x rows.  Rows are walked one after the
 // other: issuing all rows' loads first doubles the registers, halves the resident blocks and
 // ran 25 % slower.
-template <class T, class C, bool UNI>
+template <class T, class C, bool UNI, int M>
 __global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x;
   if (k >= p.Nz) return;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesH, tl.y, 8 * kMarch, 0, 1, tl.w, 32);
-  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, tl.y, 8 * kMarch, tl.w, 32);
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, tl.y, 8 * M, 0, 1, tl.w, 32);
+  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, tl.y, 8 * M, tl.w, 32);
 #pragma unroll 1
-  for (int r = 0; r < kMarch; ++r) {
+  for (int r = 0; r < M; ++r) {
     const int i = tl.y + threadIdx.y + 8 * r;
     if (fast) h_cell_2d<T, C, UNI, true>(p, i, k, false);
     else if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
   }
 }
 
-template <class T, class C, bool UNI>
+template <class T, class C, bool UNI, int M>
 __global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesE, tl.y, 8 * kMarch, 0, 1, tl.w, 32);
-  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, tl.y, 8 * kMarch, tl.w, 32);
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, tl.y, 8 * M, 0, 1, tl.w, 32);
+  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, tl.y, 8 * M, tl.w, 32);
   typename MaxBits<C>::type mbits = 0;
   if (k < p.Nz) {
 #pragma unroll 1
-    for (int r = 0; r < kMarch; ++r) {
+    for (int r = 0; r < M; ++r) {
       const int i = tl.y + threadIdx.y + 8 * r;
       typename MaxBits<C>::type b = 0;
       if (fast) b = e_cell_2d<T, C, UNI, true, true>(p, i, k, false);
@@ -1078,41 +1078,53 @@ cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s) {
 }
 
 template <class T, class C>
-cudaError_t launch_batch_tiles(const StepParams<T, C>* ps, const int* first, int n, int nblocks, bool planar, int4* tiles,
-                               cudaStream_t s) {
+cudaError_t launch_batch_tiles(const StepParams<T, C>* ps, const int* first, int n, int nblocks, bool planar, int march,
+                               int4* tiles, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  batch_tiles_kernel<T, C><<<grid1d(nblocks, 256), 256, 0, s>>>(ps, first, n, nblocks, planar ? 1 : 0, tiles);
+  batch_tiles_kernel<T, C><<<grid1d(nblocks, 256), 256, 0, s>>>(ps, first, n, nblocks, planar ? 1 : 0, march, tiles);
   return cudaGetLastError();
+}
+
+template <class T, class C, int M>
+static void batch_step_m(const StepParams<T, C>* ps, const int4* tiles, int nblocks, bool planar, bool uniform,
+                         bool h_half, cudaStream_t s) {
+  dim3 block(32, 8);
+  if (planar) {
+    if (h_half) {
+      if (uniform) h_batch_2d<T, C, true, M><<<nblocks, block, 0, s>>>(ps, tiles);
+      else h_batch_2d<T, C, false, M><<<nblocks, block, 0, s>>>(ps, tiles);
+    } else {
+      if (uniform) e_batch_2d<T, C, true, M><<<nblocks, block, 0, s>>>(ps, tiles);
+      else e_batch_2d<T, C, false, M><<<nblocks, block, 0, s>>>(ps, tiles);
+    }
+  } else {
+    if (h_half) {
+      if (uniform) h_batch_3d<T, C, true, M><<<nblocks, block, 0, s>>>(ps, tiles);
+      else h_batch_3d<T, C, false, M><<<nblocks, block, 0, s>>>(ps, tiles);
+    } else {
+      if (uniform) e_batch_3d<T, C, true, M><<<nblocks, block, 0, s>>>(ps, tiles);
+      else e_batch_3d<T, C, false, M><<<nblocks, block, 0, s>>>(ps, tiles);
+    }
+  }
 }
 
 template <class T, class C>
 cudaError_t launch_batch_step(const StepParams<T, C>* ps, const int4* tiles, int nblocks, bool planar, bool uniform,
-                              bool h_half, cudaStream_t s) {
+                              int march, bool h_half, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  dim3 block(32, 8);
-  if (planar) {
-    if (h_half) {
-      if (uniform) h_batch_2d<T, C, true><<<nblocks, block, 0, s>>>(ps, tiles);
-      else h_batch_2d<T, C, false><<<nblocks, block, 0, s>>>(ps, tiles);
-    } else {
-      if (uniform) e_batch_2d<T, C, true><<<nblocks, block, 0, s>>>(ps, tiles);
-      else e_batch_2d<T, C, false><<<nblocks, block, 0, s>>>(ps, tiles);
-    }
-  } else {
-    if (h_half) {
-      if (uniform) h_batch_3d<T, C, true><<<nblocks, block, 0, s>>>(ps, tiles);
-      else h_batch_3d<T, C, false><<<nblocks, block, 0, s>>>(ps, tiles);
-    } else {
-      if (uniform) e_batch_3d<T, C, true><<<nblocks, block, 0, s>>>(ps, tiles);
-      else e_batch_3d<T, C, false><<<nblocks, block, 0, s>>>(ps, tiles);
-    }
+  switch (march) {
+    case 1: batch_step_m<T, C, 1>(ps, tiles, nblocks, planar, uniform, h_half, s); break;
+    case 2: batch_step_m<T, C, 2>(ps, tiles, nblocks, planar, uniform, h_half, s); break;
+    case 4: batch_step_m<T, C, 4>(ps, tiles, nblocks, planar, uniform, h_half, s); break;
+    case 8: batch_step_m<T, C, 8>(ps, tiles, nblocks, planar, uniform, h_half, s); break;
+    default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
-int batch_blocks(int Nx, int Ny, int Nz, bool planar) {
-  if (planar) return ((Nz + 31) / 32) * ((Nx + 8 * kMarch - 1) / (8 * kMarch));
-  return ((Nz + 31) / 32) * ((Ny + 7) / 8) * ((Nx + kMarch3 - 1) / kMarch3);
+int batch_blocks(int Nx, int Ny, int Nz, bool planar, int march) {
+  if (planar) return ((Nz + 31) / 32) * ((Nx + 8 * march - 1) / (8 * march));
+  return ((Nz + 31) / 32) * ((Ny + 7) / 8) * ((Nx + march - 1) / march);
 }
 
 cudaError_t launch_block_map(const int* first, int n, int nblocks, int2* map, cudaStream_t s) {
@@ -1159,9 +1171,9 @@ cudaError_t launch_dft_flux(const double* acc, int nfreq, long long ncell, doubl
                                          double, cudaStream_t);                                                        \
   template cudaError_t launch_probes<T>(const ProbeParams&, T* const[6], double*, cudaStream_t);                   \
   template cudaError_t launch_dft<T>(const DftParams&, T* const[4], cudaStream_t);                                 \
-  template cudaError_t launch_batch_tiles<T, C>(const StepParams<T, C>*, const int*, int, int, bool, int4*,         \
+  template cudaError_t launch_batch_tiles<T, C>(const StepParams<T, C>*, const int*, int, int, bool, int, int4*,    \
                                                 cudaStream_t);                                                     \
-  template cudaError_t launch_batch_step<T, C>(const StepParams<T, C>*, const int4*, int, bool, bool, bool,     \
+  template cudaError_t launch_batch_step<T, C>(const StepParams<T, C>*, const int4*, int, bool, bool, int, bool,     \
                                                cudaStream_t);                                                          \
   template cudaError_t launch_dft_batch<T>(const DftParams*, const int2*, int, const int*, cudaStream_t);
 LX_INST(double, double)

@@ -27,13 +27,14 @@ cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s);
 // Batched updates: member m of a group owns blocks [first[m], first[m+1]) of each launch;
 // launch_batch_tiles turns that prefix into the per-block tile map the update kernels read.
 template <class T, class C>
-cudaError_t launch_batch_tiles(const StepParams<T, C>* ps, const int* first, int n, int nblocks, bool planar, int4* tiles,
-                               cudaStream_t s);
+cudaError_t launch_batch_tiles(const StepParams<T, C>* ps, const int* first, int n, int nblocks, bool planar, int march,
+                               int4* tiles, cudaStream_t s);
 template <class T, class C>
 cudaError_t launch_batch_step(const StepParams<T, C>* ps, const int4* tiles, int nblocks, bool planar, bool uniform,
-                              bool h_half, cudaStream_t s);
-// blocks one member occupies in a batched update launch
-int batch_blocks(int Nx, int Ny, int Nz, bool planar);
+                              int march, bool h_half, cudaStream_t s);
+// blocks one member occupies in a batched update launch; march = cells each thread walks
+// along x (planar: rows 8 apart; 3-D: planes), one of 1, 2, 4, 8
+int batch_blocks(int Nx, int Ny, int Nz, bool planar, int march);
 // block -> {member, block within the member} for a prefix `first` of n members
 cudaError_t launch_block_map(const int* first, int n, int nblocks, int2* map, cudaStream_t s);
 template <class C>

@@ -322,6 +322,21 @@ class Batch:
     def wait(self) -> None:
         self._check(self.lib.lx_batch_wait(self.h))
 
+    def set_march(self, planar_rows: int, planes_3d: int) -> None:
+        """Cells each thread of the batched kernels walks along x (1, 2, 4 or 8)."""
+        self._check(self.lib.lx_batch_set_march(self.h, planar_rows, planes_3d))
+
+    def march(self) -> tuple:
+        a, b = C.c_int(), C.c_int()
+        self._check(self.lib.lx_batch_get_march(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def autotune(self, steps: int = 20) -> tuple:
+        """Times each march on twins of the members and keeps the fastest; returns (planar, 3-D)."""
+        a, b = C.c_int(), C.c_int()
+        self._check(self.lib.lx_batch_autotune(self.h, steps, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def __len__(self):
         return self.lib.lx_batch_size(self.h)
 

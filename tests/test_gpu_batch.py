@@ -117,3 +117,47 @@ def test_batch_async_equals_blocking(engine):
         _same(m, t)
     ba.close()
     bb.close()
+
+
+@pytest.mark.parametrize("march", [1, 2, 8])
+def test_batch_tile_shape_does_not_change_results(engine, march):
+    from luxum_gb300 import Batch
+
+    members = [_make(n, 1) for n in NAMES]
+    twins = [_make(n, 1) for n in NAMES]
+    batch = Batch(chunk=10)
+    batch.set_march(march, march)
+    for m in members:
+        batch.add(m)
+    batch.step(37)
+    for t in twins:
+        t.step(37)
+    for m, t in zip(members, twins):
+        _same(m, t)
+    batch.close()
+
+
+def test_batch_autotune_leaves_members_untouched(engine):
+    from luxum_gb300 import Batch
+
+    members = [_make(n, 1) for n in NAMES]
+    twins = [_make(n, 1) for n in NAMES]
+    batch = Batch(chunk=10)
+    for m in members:
+        batch.add(m)
+    batch.step(13)
+    before = [[m.field(c) if np.prod(m.shape(c)) else None for c in range(6)] for m in members]
+    got = batch.autotune(10)
+    assert got[0] in (1, 2, 4, 8) and got[1] in (1, 2, 4, 8)
+    assert batch.march() == got
+    for m, f in zip(members, before):
+        assert m.t == 13
+        for c in range(6):
+            if f[c] is not None:
+                assert np.array_equal(m.field(c), f[c])
+    batch.step(24)
+    for t in twins:
+        t.step(37)
+    for m, t in zip(members, twins):
+        _same(m, t)
+    batch.close()
