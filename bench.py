@@ -233,8 +233,33 @@ def lens_sims(n_sims: int, seed: int, precision: int, steps: int):
     return sims
 
 
+def box_sims(n_sims: int, seed: int, precision: int, steps: int):
+    """3-D batch workload: cubes of side U{64..192} (seeded), the serving requests' 3-D form:
+    textbook CPML of min(16, side/8) cells, an Ez plane wave along x through a TF/SF box as
+    deep again, and 1-4 dielectric boxes with eps_r ~ U(1, 12)."""
+    from luxum_gb300 import Sim
+
+    rng = np.random.default_rng(seed)
+    sims = []
+    for q in range(n_sims):
+        n = int(rng.integers(64, 193))
+        m = serve_margin(n)
+        p = serve_params({"side": n, "planar": False})
+        p.precision = precision
+        p.num_timesteps = steps
+        s = Sim(p)
+        for _ in range(int(rng.integers(1, 5))):
+            c0 = rng.integers(2 * m + 2, n - 2 * m - 8, 3)
+            w = rng.integers(4, max(5, n // 6), 3)
+            lo = np.maximum(c0 - w // 2, 2 * m + 2)
+            hi = np.minimum(c0 + w // 2, n - 2 * m - 8)
+            s.set_eps_box(tuple(int(v) for v in lo), tuple(int(v) for v in hi), float(rng.uniform(1.0, 12.0)))
+        sims.append(s)
+    return sims
+
+
 def bench_batch(args):
-    """--config batch: 256 uneven planar simulations stepped as one batch."""
+    """--config batch: 256 uneven planar simulations stepped as one batch (batch3d: 3-D cubes)."""
     import torch
 
     import __graft_entry__
@@ -243,8 +268,9 @@ def bench_batch(args):
     from luxum_gb300 import Batch
 
     steps = args.batch_steps
-    sims = lens_sims(args.batch_sims, 4, 1, steps)
-    cells = sum(s.p.Nx * s.p.Nz for s in sims)
+    three = args.config == "batch3d"
+    sims = box_sims(args.batch_sims, 6, 1, steps) if three else lens_sims(args.batch_sims, 4, 1, steps)
+    cells = sum(s.p.Nx * s.p.Ny * s.p.Nz for s in sims)
     batch = Batch(chunk=100)
     for s in sims:
         batch.add(s)
@@ -268,7 +294,7 @@ def bench_batch(args):
     value = cells * steps * args.steps / dt / 1e9
     # the same simulations one by one (unbatched), on a sample
     sample = sims[: args.solo_sample]
-    scells = sum(s.p.Nx * s.p.Nz for s in sample)
+    scells = sum(s.p.Nx * s.p.Ny * s.p.Nz for s in sample)
     for s in sample:
         s.reset()
         s.step(100)
@@ -279,8 +305,11 @@ def bench_batch(args):
         s.step(args.solo_steps)
         s.sync()
     solo = scells * args.solo_steps / (time.perf_counter() - t0) / 1e9
-    line = {"config": {"workload": f"batch of {len(sims)} planar lens simulations, sides U{{128..1024}} seed 4, "
-                                   f"CPML 16, TF/SF normal incidence, FP32, {steps} steps, graph chunks of 100",
+    desc = (f"batch of {len(sims)} 3-D simulations, cubes of side U{{64..192}} seed 6, CPML min(16, side/8), TF/SF "
+            f"plane wave, 1-4 eps boxes, FP32, {steps} steps, graph chunks of 100" if three else
+            f"batch of {len(sims)} planar lens simulations, sides U{{128..1024}} seed 4, "
+            f"CPML 16, TF/SF normal incidence, FP32, {steps} steps, graph chunks of 100")
+    line = {"config": {"workload": desc,
                        "cells": cells, "cell_updates_per_run": cells * steps},
             "metric": "Gcell-updates/s (batched)", "value": value, "unit": UNIT, "runs": args.steps,
             "s_per_run": dt / args.steps, "dtype": "f32",
@@ -562,7 +591,7 @@ def main():
                     help="run the N^3 profiling case instead of the benchmark (for ncu)")
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--precision", type=int, default=0, help="profiling case precision: 0 fp64, 1 fp32, 2 fp16")
-    ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "serve", "phc"],
+    ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "batch3d", "serve", "phc"],
                     help="drop-in: the headline 256^3 FP64 workload; batch: 256 uneven planar simulations")
     ap.add_argument("--batch-sims", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=3000)
@@ -573,7 +602,9 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-chunk", type=int, default=100)
     args = ap.parse_args()
-    if args.config == "batch":
+    if args.config in ("batch", "batch3d"):
+        if args.config == "batch3d" and args.batch_sims == 256:
+            args.batch_sims, args.batch_steps = 48, 1000
         return bench_batch(args)
     if args.config == "serve":
         return bench_serve(args)

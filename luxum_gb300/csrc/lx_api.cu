@@ -229,6 +229,13 @@ static PatchSet mkset(const lx_sim* s, int axis, int pl0, int pl1, double pos0, 
   ps.dn = dn;
   ps.hcurl = hcurl;
   ps.scale = hcurl ? s->hscale : 1.0;
+  // the constant part of every entry of this set, in the order the reference applies it
+  // (maxwell.cc:289 and siblings: * E_dir / d, or / d / c / mu0 for the H-curl lines)
+  double f = neg * dir / dn;
+  if (hcurl) f = f / s->k.c / s->k.mew0;
+  if (s->uniform) f = f * dn;  // difference units
+  if (ps.scale != 1.0) f = f * ps.scale;
+  ps.factor = f;
   bool empty = false;
   for (int b = 0; b < 3; b++) {
     ps.lo[b] = lo[b];
@@ -1325,6 +1332,7 @@ static lx::PrologueParams make_prologue(lx_sim* s) {
   pp.dx = s->k.dx; pp.dy = s->k.dy; pp.dz = s->k.dz;
   pp.kx = s->k.k[0]; pp.ky = s->k.k[1]; pp.kz = s->k.k[2];
   pp.init = s->k.init; pp.c = s->k.c; pp.dt = s->k.dt; pp.mu0 = s->k.mew0; pp.pw_sigma = s->k.sigma;
+  pp.inv_sigma = 1.0 / s->k.sigma;
   pp.scale_units = s->uniform ? 0.0 : 1.0;
   pp.src_kind = s->src_kind;
   pp.src_idx = s->src_idx;

@@ -62,6 +62,9 @@ struct PatchSet {
   double dn;         // spacing along `axis` (the reference divides by it)
   int hcurl;         // 1: also divide by c and mu0 (H-curl lines)
   double scale;      // stored-H scale for H-curl lines (1 unless H is stored scaled)
+  // neg * dir / dn (/ c / mu0 for H-curl lines) (* dn in difference units) * scale, formed
+  // once on the host: a table entry is exp(-X^2 / sigma) * factor, signed per plane
+  double factor;
 };
 
 // Parameters of the step prologue: TF/SF tables, point source, monitor reset.
@@ -72,6 +75,7 @@ struct PrologueParams {
   int tab_total;      // total entries over all active sets
   int planar;
   double dx, dy, dz, kx, ky, kz, init, c, dt, mu0, pw_sigma;
+  double inv_sigma;    // 1 / pw_sigma
   double scale_units;  // 1 (curl units) or 0 = scale each entry by its plane spacing (difference units)
   int t;
   // point source
