@@ -114,6 +114,7 @@ __device__ __forceinline__ long long psi_index(int axis, const Slab& s, int si_,
 
 // ------------------------------------------------------------------ prologue
 
+// The entry before its plane's sign (curl - v or curl + v).
 __device__ double incident_value(const PrologueParams& p, const PatchSet& ps, int plane, int e, int t) {
   // table entry e of `plane` -> in-plane indices -> wave positions
   double pos[3];
@@ -142,8 +143,7 @@ __device__ double incident_value(const PrologueParams& p, const PatchSet& ps, in
   // exp(-X^2/sigma) times the set's constant factor: one exp and two multiplies per entry
   // (the reference divides by sigma, d, c and mu0 in turn; the products differ from its
   // quotients in the last bit only)
-  const double v = __dmul_rn(exp(-__dmul_rn(__dmul_rn(X, X), p.inv_sigma)), ps.factor);
-  return ps.sign[plane] < 0 ? -v : v;
+  return __dmul_rn(exp(-__dmul_rn(__dmul_rn(X, X), p.inv_sigma)), ps.factor);
 }
 
 template <class C>
@@ -169,20 +169,36 @@ __device__ __forceinline__ void prologue_body(const PrologueParams& p, const int
       }
     }
   }
-  for (int e = gid; e < p.tab_total; e += gstride) {
-    int rem = e;
-    for (int s = 0; s < p.nsets; ++s) {
-      const PatchSet& ps = p.sets[s];
-      if (!ps.active) continue;
-      const int len = 2 * ps.plane_len;
-      if (rem < len) {
-        const int plane = rem >= ps.plane_len ? 1 : 0;
-        const double v = incident_value(p, ps, plane, rem - plane * ps.plane_len, t);
-        tab_out[ps.tab + rem] = (C)v;
-        break;
-      }
-      rem -= len;
-    }
+  // Work items: one per entry, except that a set whose planes are normal to an axis k has no
+  // component along shares its values between the two planes (the normal position is
+  // multiplied by 0 in X), so one item writes both.  The sets' work ranges are staged in
+  // shared memory once per block, so an item finds its set without a walk through the
+  // parameter block in global memory.
+  __shared__ int w_end[12];
+  __shared__ unsigned char w_shared[12];
+  if (threadIdx.x < 12) {  // one thread per set: the loads run in parallel
+    const int s = threadIdx.x;
+    const double kn[3] = {p.kx, p.ky, p.kz};
+    const bool on = p.tab_total > 0 && s < p.nsets && p.sets[s].active;
+    const bool sh = on && kn[p.sets[s].axis] == 0.0;
+    w_end[s] = on ? (sh ? 1 : 2) * p.sets[s].plane_len : 0;
+    w_shared[s] = sh;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int s = 1; s < 12; ++s) w_end[s] += w_end[s - 1];
+  __syncthreads();
+  const int work = w_end[11];
+  for (int e = gid; e < work; e += gstride) {
+    int s = 0;
+    while (e >= w_end[s]) ++s;
+    const PatchSet& ps = p.sets[s];
+    const int rem = e - (s ? w_end[s - 1] : 0);
+    const int plane = rem >= ps.plane_len ? 1 : 0;
+    const int q = rem - plane * ps.plane_len;
+    const double v = incident_value(p, ps, plane, q, t);
+    tab_out[ps.tab + plane * ps.plane_len + q] = (C)(ps.sign[plane] < 0 ? -v : v);
+    if (w_shared[s]) tab_out[ps.tab + ps.plane_len + q] = (C)(ps.sign[1] < 0 ? -v : v);
   }
 }
 
