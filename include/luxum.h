@@ -274,7 +274,7 @@ LX_API lx_status lx_batch_step(lx_batch* b, int nsteps);
 LX_API lx_status lx_batch_step_async(lx_batch* b, int nsteps);
 LX_API lx_status lx_batch_wait(lx_batch* b);
 /* Tile shape of the batched update kernels: cells each thread walks along x, for planar
- * members (rows 8 apart) and for 3-D members (planes); each 1, 2, 4 or 8 (defaults 8, 4).
+ * members (rows 8 apart) and for 3-D members (planes); each 1, 2, 4 or 8 (defaults 8, 8).
  * Results do not depend on it, only speed. */
 LX_API lx_status lx_batch_set_march(lx_batch* b, int planar_rows, int planes_3d);
 LX_API lx_status lx_batch_get_march(const lx_batch* b, int* planar_rows, int* planes_3d);

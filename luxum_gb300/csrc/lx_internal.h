@@ -25,10 +25,10 @@ namespace lx {
 constexpr int kMaxProbes = 64;
 constexpr int kMaxDftFreq = 256;
 // Default cells each thread of a batched update kernel walks through along x: planar rows 8
-// apart, and 3-D planes (the autotuner's picks on the lens and serving workloads);
+// apart, and 3-D planes (the autotuner's picks on the lens and 3-D cube workloads);
 // lx_batch_autotune picks per batch among 1, 2, 4 and 8.
 constexpr int kMarch2 = 8;
-constexpr int kMarch3 = 4;
+constexpr int kMarch3 = 8;
 
 // Packed CPML slab along one axis.
 struct Slab {
