@@ -370,34 +370,27 @@ __device__ __forceinline__ void h_cell_3d(const StepParams<T, C>& p, const int i
   h_apply<T, C, UNI, FAST>(p, i, j, k, tf, v);
 }
 
-// Each block owns a 32 (z) x 8 (y) column of cells over M consecutive x planes; each
-// thread walks its column through the planes, so index set-up and the TF/SF tile test are
-// paid once per M cells.
 // Resident blocks per SM asked of the compiler for the H kernel (a register cap): 8 for
-// float compute (32 registers, no spills; FP16 storage 14 % faster than at 40 registers),
-// 5 for FP64 (its natural 48 registers; an explicit 1 lets the compiler take 54).
+// float compute (32 registers, 12-16 bytes spilled; FP16 storage 14 % faster than at 40
+// registers), 5 for FP64 (its natural 48 registers; an explicit 1 lets the compiler take 54).
 template <class C>
 struct HMinBlocks {
   static constexpr int v = sizeof(C) == 4 ? 8 : 5;
 };
 
-template <class T, class C, bool UNI, int M>
+// One cell per thread; a block is 32 (z) x 8 (y) cells of one x plane.  Blocks whose tile is
+// interior take the cell code with every condition decided at compile time.
+template <class T, class C, bool UNI>
 __global__ void __launch_bounds__(256, HMinBlocks<C>::v) h_kernel_3d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
-  const int i0 = blockIdx.z * M;
+  const int i = blockIdx.z;
   if (k >= p.Nz || j >= p.Ny) return;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i0, M, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
-  if constexpr (M == 1) {
-    if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i0, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32))
-      h_cell_3d<T, C, UNI, true>(p, i0, j, k, false);
-    else
-      h_cell_3d<T, C, UNI>(p, i0, j, k, tf);
-  } else {
-    const int i1 = min(i0 + M, p.Nx);
-#pragma unroll 1
-    for (int i = i0; i < i1; ++i) h_cell_3d<T, C, UNI>(p, i, j, k, tf);
-  }
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
+  if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32))
+    h_cell_3d<T, C, UNI, true>(p, i, j, k, false);
+  else
+    h_cell_3d<T, C, UNI>(p, i, j, k, tf);
 }
 
 // E half-step over cell (i,j,k) for Ex, Ey, Ez (three_dim_pml.cc:218-276, three_dim.cc:134-189).
@@ -513,26 +506,15 @@ __device__ __forceinline__ typename MaxBits<C>::type e_cell_3d(const StepParams<
   return e_apply<T, C, UNI, MON, FAST>(p, i, j, k, tf, v);
 }
 
-template <class T, class C, bool UNI, bool MON, int M>
+template <class T, class C, bool UNI, bool MON>
 __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
-  const int i0 = blockIdx.z * M;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i0, M, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
+  const int i = blockIdx.z;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
   typename MaxBits<C>::type mbits = 0;
-  if (k < p.Nz && j < p.Ny) {
-    if constexpr (M == 1) {
-      // (the interior fast path gains nothing here and costs FP16 storage 9 %)
-      mbits = e_cell_3d<T, C, UNI, MON>(p, i0, j, k, tf);
-    } else {
-      const int i1 = min(i0 + M, p.Nx);
-#pragma unroll 1
-      for (int i = i0; i < i1; ++i) {
-        const typename MaxBits<C>::type b = e_cell_3d<T, C, UNI, MON>(p, i, j, k, tf);
-        mbits = b > mbits ? b : mbits;
-      }
-    }
-  }
+  // (the interior fast path gains nothing here and costs FP16 storage 9 %)
+  if (k < p.Nz && j < p.Ny) mbits = e_cell_3d<T, C, UNI, MON>(p, i, j, k, tf);
   if (MON && p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
 
@@ -602,20 +584,17 @@ __device__ __forceinline__ void h_cell_2d(const StepParams<T, C>& p, const int i
   h2_apply<T, C, UNI, FAST>(p, i, k, tf, v);
 }
 
-// Each block owns 32 (z) x 8*M (x) cells; thread row r handles x rows r, r+8, ...
-template <class T, class C, bool UNI, int M>
+// One cell per thread; a block is 32 (z) x 8 (x) cells.
+template <class T, class C, bool UNI>
 __global__ void __launch_bounds__(256) h_kernel_2d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
-  const int ib = blockIdx.y * 8 * M;
-  if (k >= p.Nz) return;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesH, ib, 8 * M, 0, 1, blockIdx.x * 32, 32);
-  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, ib, 8 * M, blockIdx.x * 32, 32);
-#pragma unroll 1
-  for (int r = 0; r < M; ++r) {
-    const int i = ib + threadIdx.y + 8 * r;
-    if (fast) h_cell_2d<T, C, UNI, true>(p, i, k, false);
-    else if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
-  }
+  const int ib = blockIdx.y * 8, i = ib + threadIdx.y;
+  if (k >= p.Nz || i >= p.Nx) return;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesH, ib, 8, 0, 1, blockIdx.x * 32, 32);
+  if (!tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, ib, 8, blockIdx.x * 32, 32))
+    h_cell_2d<T, C, UNI, true>(p, i, k, false);
+  else
+    h_cell_2d<T, C, UNI>(p, i, k, tf);
 }
 
 // Planar E half-step: Ey (two_dim_pml.cc:164-181, two_dim.cc:113-128).  The reference loop
@@ -677,22 +656,16 @@ __device__ __forceinline__ typename MaxBits<C>::type e_cell_2d(const StepParams<
   return e2_apply<T, C, UNI, MON, FAST>(p, i, k, tf, v);
 }
 
-template <class T, class C, bool UNI, bool MON, int M>
+template <class T, class C, bool UNI, bool MON>
 __global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
   const int k = blockIdx.x * 32 + threadIdx.x;
-  const int ib = blockIdx.y * 8 * M;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesE, ib, 8 * M, 0, 1, blockIdx.x * 32, 32);
-  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, ib, 8 * M, blockIdx.x * 32, 32);
+  const int ib = blockIdx.y * 8, i = ib + threadIdx.y;
+  const bool tf = p.tfsf && tile_meets_planes(p.planesE, ib, 8, 0, 1, blockIdx.x * 32, 32);
+  const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, ib, 8, blockIdx.x * 32, 32);
   typename MaxBits<C>::type mbits = 0;
-  if (k < p.Nz) {
-#pragma unroll 1
-    for (int r = 0; r < M; ++r) {
-      const int i = ib + threadIdx.y + 8 * r;
-      typename MaxBits<C>::type b = 0;
-      if (fast) b = e_cell_2d<T, C, UNI, MON, true>(p, i, k, false);
-      else if (i < p.Nx) b = e_cell_2d<T, C, UNI, MON>(p, i, k, tf);
-      mbits = b > mbits ? b : mbits;
-    }
+  if (k < p.Nz && i < p.Nx) {
+    if (fast) mbits = e_cell_2d<T, C, UNI, MON, true>(p, i, k, false);
+    else mbits = e_cell_2d<T, C, UNI, MON>(p, i, k, tf);
   }
   if (MON && p.max_slot) block_max_atomic(mbits, p.max_slot);
 }
@@ -1028,32 +1001,31 @@ template <class T, class C>
 cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bool h_half, cudaStream_t s) {
   // single simulations: one cell per thread (their parameters sit in the constant bank, and
   // walking several cells raises register use past what pays off)
-  constexpr int M = 1;
   dim3 block(32, 8);
   const bool mon = p.max_slot || p.etotal;
   if (planar) {
-    dim3 grid((p.Nz + 31) / 32, (p.Nx + 8 * M - 1) / (8 * M), 1);
+    dim3 grid((p.Nz + 31) / 32, (p.Nx + 7) / 8, 1);
     if (h_half) {
-      if (uniform) h_kernel_2d<T, C, true, M><<<grid, block, 0, s>>>(p);
-      else h_kernel_2d<T, C, false, M><<<grid, block, 0, s>>>(p);
+      if (uniform) h_kernel_2d<T, C, true><<<grid, block, 0, s>>>(p);
+      else h_kernel_2d<T, C, false><<<grid, block, 0, s>>>(p);
     } else if (mon) {
-      if (uniform) e_kernel_2d<T, C, true, true, M><<<grid, block, 0, s>>>(p);
-      else e_kernel_2d<T, C, false, true, M><<<grid, block, 0, s>>>(p);
+      if (uniform) e_kernel_2d<T, C, true, true><<<grid, block, 0, s>>>(p);
+      else e_kernel_2d<T, C, false, true><<<grid, block, 0, s>>>(p);
     } else {
-      if (uniform) e_kernel_2d<T, C, true, false, M><<<grid, block, 0, s>>>(p);
-      else e_kernel_2d<T, C, false, false, M><<<grid, block, 0, s>>>(p);
+      if (uniform) e_kernel_2d<T, C, true, false><<<grid, block, 0, s>>>(p);
+      else e_kernel_2d<T, C, false, false><<<grid, block, 0, s>>>(p);
     }
   } else {
-    dim3 grid((p.Nz + 31) / 32, (p.Ny + 7) / 8, (p.Nx + M - 1) / M);
+    dim3 grid((p.Nz + 31) / 32, (p.Ny + 7) / 8, p.Nx);
     if (h_half) {
-      if (uniform) h_kernel_3d<T, C, true, M><<<grid, block, 0, s>>>(p);
-      else h_kernel_3d<T, C, false, M><<<grid, block, 0, s>>>(p);
+      if (uniform) h_kernel_3d<T, C, true><<<grid, block, 0, s>>>(p);
+      else h_kernel_3d<T, C, false><<<grid, block, 0, s>>>(p);
     } else if (mon) {
-      if (uniform) e_kernel_3d<T, C, true, true, M><<<grid, block, 0, s>>>(p);
-      else e_kernel_3d<T, C, false, true, M><<<grid, block, 0, s>>>(p);
+      if (uniform) e_kernel_3d<T, C, true, true><<<grid, block, 0, s>>>(p);
+      else e_kernel_3d<T, C, false, true><<<grid, block, 0, s>>>(p);
     } else {
-      if (uniform) e_kernel_3d<T, C, true, false, M><<<grid, block, 0, s>>>(p);
-      else e_kernel_3d<T, C, false, false, M><<<grid, block, 0, s>>>(p);
+      if (uniform) e_kernel_3d<T, C, true, false><<<grid, block, 0, s>>>(p);
+      else e_kernel_3d<T, C, false, false><<<grid, block, 0, s>>>(p);
     }
   }
   return cudaGetLastError();
