@@ -1832,8 +1832,9 @@ static lx_status batch_rebuild(lx_batch* b) {
 template <class T, class C>
 static lx_status batch_enqueue(lx_batch* b, long long step0, int nsteps) {
   const int n = (int)b->sims.size();
+  // the members' device step counters advance once, after the chunk; step q runs at ts + q
   for (int q = 0; q < nsteps; q++) {
-    BCK(lx::launch_prologue_batch<C>(b->d_pps, b->d_ts, n, b->max_entries, b->stream));
+    BCK(lx::launch_prologue_batch<C>(b->d_pps, b->d_ts, q, n, b->max_entries, b->stream));
     for (auto& g : b->groups)
       BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.nblocks, g.planar,
                                       g.uniform, g.march, true, b->stream));
@@ -1843,9 +1844,9 @@ static lx_status batch_enqueue(lx_batch* b, long long step0, int nsteps) {
     const long long bs = step0 + q;
     for (auto& cl : b->dft)
       if (bs % cl.every == cl.phase)
-        BCK(lx::launch_dft_batch<T>(cl.d_planes, cl.d_map, cl.nblocks, b->d_ts, b->stream));
-    BCK(lx::launch_tick(b->d_ts, n, b->stream));
+        BCK(lx::launch_dft_batch<T>(cl.d_planes, cl.d_map, cl.nblocks, b->d_ts, q, b->stream));
   }
+  if (nsteps > 0) BCK(lx::launch_tick(b->d_ts, n, nsteps, b->stream));
   return LX_OK;
 }
 

@@ -207,17 +207,18 @@ __global__ void prologue_kernel(const PrologueParams p, C* tab_out) {
   prologue_body<C>(p, p.t, tab_out, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
-// Batched prologue: blockIdx.y selects the simulation; its step counter lives on the device
-// so that a captured chunk of steps can be replayed.
+// Batched prologue: blockIdx.y selects the simulation.  Its step counter lives on the device
+// and advances once per chunk, so that a captured chunk can be replayed: step k of a chunk
+// runs at ts[sim] + k.
 template <class C>
-__global__ void prologue_batch_kernel(const PrologueParams* __restrict__ pps, const int* __restrict__ ts) {
+__global__ void prologue_batch_kernel(const PrologueParams* __restrict__ pps, const int* __restrict__ ts, int k) {
   const PrologueParams& p = pps[blockIdx.y];
-  prologue_body<C>(p, ts[blockIdx.y], (C*)p.tab, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+  prologue_body<C>(p, ts[blockIdx.y] + k, (C*)p.tab, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
-__global__ void tick_kernel(int* ts, int n) {
+__global__ void tick_kernel(int* ts, int n, int steps) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n) ts[s] += 1;
+  if (s < n) ts[s] += steps;
 }
 
 // ------------------------------------------------------------------ monitor
@@ -943,10 +944,11 @@ __global__ void dft_kernel(const DftParams d, const T* f0, const T* f1, const T*
 // Batched DFT planes: a flat launch over the planes sampled at this step; bfirst[q] is the
 // first block of plane q (each block serves one plane, so its phase table is per plane).
 template <class T>
-__global__ void dft_batch_kernel(const DftParams* __restrict__ ds, const int2* __restrict__ map, const int* __restrict__ ts) {
+__global__ void dft_batch_kernel(const DftParams* __restrict__ ds, const int2* __restrict__ map, const int* __restrict__ ts,
+                                 int k) {
   const int2 bm = map[blockIdx.x];
   const DftParams& d = ds[bm.x];
-  const int t = ts[d.sim];
+  const int t = ts[d.sim] + k;
   if (t % d.every_ != 0) return;
   dft_body<T>(d, t, (const T*)d.f[0], (const T*)d.f[1], (const T*)d.f[2], (const T*)d.f[3], bm.y);
 }
@@ -1127,25 +1129,26 @@ cudaError_t launch_block_map(const int* first, int n, int nblocks, int2* map, cu
 }
 
 template <class C>
-cudaError_t launch_prologue_batch(const PrologueParams* pps, const int* ts, int nsims, int max_entries, cudaStream_t s) {
+cudaError_t launch_prologue_batch(const PrologueParams* pps, const int* ts, int k, int nsims, int max_entries,
+                                  cudaStream_t s) {
   if (nsims <= 0) return cudaSuccess;
   long long gx = (max_entries + 255) / 256;
   if (gx < 1) gx = 1;
   if (gx > 1024) gx = 1024;
-  prologue_batch_kernel<C><<<dim3((unsigned)gx, (unsigned)nsims), 256, 0, s>>>(pps, ts);
+  prologue_batch_kernel<C><<<dim3((unsigned)gx, (unsigned)nsims), 256, 0, s>>>(pps, ts, k);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tick(int* ts, int n, cudaStream_t s) {
+cudaError_t launch_tick(int* ts, int n, int steps, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  tick_kernel<<<(n + 255) / 256, 256, 0, s>>>(ts, n);
+  tick_kernel<<<(n + 255) / 256, 256, 0, s>>>(ts, n, steps);
   return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nblocks, const int* ts, cudaStream_t s) {
+cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nblocks, const int* ts, int k, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  dft_batch_kernel<T><<<nblocks, 256, 0, s>>>(ds, map, ts);
+  dft_batch_kernel<T><<<nblocks, 256, 0, s>>>(ds, map, ts, k);
   return cudaGetLastError();
 }
 
@@ -1168,14 +1171,14 @@ cudaError_t launch_dft_flux(const double* acc, int nfreq, long long ncell, doubl
                                                 cudaStream_t);                                                     \
   template cudaError_t launch_batch_step<T, C>(const StepParams<T, C>*, const int4*, int, bool, bool, int, bool,     \
                                                cudaStream_t);                                                          \
-  template cudaError_t launch_dft_batch<T>(const DftParams*, const int2*, int, const int*, cudaStream_t);
+  template cudaError_t launch_dft_batch<T>(const DftParams*, const int2*, int, const int*, int, cudaStream_t);
 LX_INST(double, double)
 LX_INST(float, float)
 LX_INST(__half, float)
 template cudaError_t launch_prologue<double>(const PrologueParams&, cudaStream_t);
 template cudaError_t launch_prologue<float>(const PrologueParams&, cudaStream_t);
-template cudaError_t launch_prologue_batch<double>(const PrologueParams*, const int*, int, int, cudaStream_t);
-template cudaError_t launch_prologue_batch<float>(const PrologueParams*, const int*, int, int, cudaStream_t);
+template cudaError_t launch_prologue_batch<double>(const PrologueParams*, const int*, int, int, int, cudaStream_t);
+template cudaError_t launch_prologue_batch<float>(const PrologueParams*, const int*, int, int, int, cudaStream_t);
 template cudaError_t launch_eps_box<double>(double*, const int[3], int, int, const int[3], const int[3], double,
                                             cudaStream_t);
 template cudaError_t launch_eps_box<float>(float*, const int[3], int, int, const int[3], const int[3], double,

@@ -38,10 +38,12 @@ int batch_blocks(int Nx, int Ny, int Nz, bool planar, int march);
 // block -> {member, block within the member} for a prefix `first` of n members
 cudaError_t launch_block_map(const int* first, int n, int nblocks, int2* map, cudaStream_t s);
 template <class C>
-cudaError_t launch_prologue_batch(const PrologueParams* pps, const int* ts, int nsims, int max_entries, cudaStream_t s);
-cudaError_t launch_tick(int* ts, int n, cudaStream_t s);
+// step k of a chunk runs at ts[sim] + k; launch_tick advances ts by the chunk's steps
+cudaError_t launch_prologue_batch(const PrologueParams* pps, const int* ts, int k, int nsims, int max_entries,
+                                  cudaStream_t s);
+cudaError_t launch_tick(int* ts, int n, int steps, cudaStream_t s);
 template <class T>
-cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nblocks, const int* ts, cudaStream_t s);
+cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nblocks, const int* ts, int k, cudaStream_t s);
 cudaError_t launch_dft_flux(const double* acc, int nfreq, long long ncell, double* part, double dA, double* out,
                             cudaStream_t s);
 

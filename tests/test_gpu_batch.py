@@ -40,7 +40,7 @@ def _same(a, b):
     assert a.t == b.t
 
 
-@pytest.mark.parametrize("precision", [1, 0])
+@pytest.mark.parametrize("precision", [1, 0, 2])
 def test_batch_equals_solo(engine, precision):
     from luxum_gb300 import Batch
 

@@ -148,3 +148,36 @@ def test_server_material_arrays(engine):
         for c in range(6):
             if np.prod(s.shape(c)):
                 assert np.array_equal(g.field(c), s.field(c)), c
+
+
+def test_server_destroy_with_work_in_flight(engine):
+    """Destroying a server cancels what is queued and running and frees every handle."""
+    from luxum_gb300 import Server
+
+    p = _params("planar_oblique")
+    srv = Server(chunk=10, max_running=1)
+    ids = [srv.submit(p, 100000) for _ in range(3)]
+    while srv.state(ids[0]) != "running":
+        srv.wait(ids[0], 0.05)
+    srv.close()  # returns after the chunk in flight
+    # a fresh server on the same device still works
+    with Server(chunk=10) as again:
+        rid = again.submit(p, 30)
+        assert again.wait(rid, 60.0) == "done"
+
+
+def test_fp16_storage_requests(engine):
+    """A server of FP16-storage requests equals the same simulations stepped alone."""
+    from luxum_gb300 import Server, Sim
+
+    p = _params("3d_pml_axis")
+    p.precision = 2
+    with Server(precision=2, chunk=16) as srv:
+        rid = srv.submit(p, 40, [((12, 10, 12), (18, 16, 20), 6.0)])
+        assert srv.wait(rid, 60.0) == "done"
+        g = srv.take(rid, p)
+    s = Sim(p)
+    s.set_eps_box((12, 10, 12), (18, 16, 20), 6.0)
+    s.step(40)
+    for c in range(6):
+        assert np.array_equal(g.field(c), s.field(c)), c
