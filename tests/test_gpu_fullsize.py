@@ -80,3 +80,31 @@ def test_3d_dropin_workload_full_grid(engine, tmp_path):
         a = g.field(c)
         assert np.array_equal(a, h.field(c)), c      # resumed run
         assert np.array_equal(a, twin.field(c)), c   # deterministic
+
+
+def test_full_grid_linearity(engine):
+    """256^3 with CPML and a dielectric cube, 1000 steps, hard CW point source: doubling the
+    source amplitude doubles every field exactly (every operation is linear and x2 is exact
+    in binary floating point while no value is subnormal, which holds in FP64 here; FP32's
+    light-cone edge reaches subnormals).  A property of the whole update at the workload's
+    full size and length, independent of the oracle."""
+    precision = 0
+    sys.path.insert(0, ROOT)
+    import bench
+    from luxum_gb300 import Sim
+
+    fields = []
+    for amp in (1.0, 2.0):
+        p = bench.workload_params(precision)
+        p.usePW = 0
+        p.usePS, p.Nx_source, p.Ny_source, p.Nz_source = 1, 128, 128, 100
+        p.amp_source, p.omega_source = amp, 2.0e9  # both kept as int by the reference
+        s = Sim(p)
+        for c in range(3):
+            s.set_material(c, bench.material(s.shape(c)), 1e6)
+        s.step(1000)
+        fields.append([s.field(c) for c in range(6)])
+        s.close()
+    for c in range(6):
+        assert np.array_equal(fields[1][c], 2.0 * fields[0][c]), c
+        assert np.abs(fields[0][c]).max() > 0
