@@ -330,7 +330,8 @@ typedef struct lx_server_stats {
 } lx_server_stats;
 
 LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_server** out);
-/* Stops the worker after the chunk in flight; running and queued requests are cancelled. */
+/* Stops the worker after the chunk in flight; running and queued requests are cancelled.
+ * No other call on the same server may run concurrently with it. */
 LX_API void lx_server_destroy(lx_server* srv);
 /* Validates and copies the request (arrays included) and queues it; *id identifies it. */
 LX_API lx_status lx_server_submit(lx_server* srv, const lx_request* req, long long* id);
@@ -340,7 +341,8 @@ LX_API lx_status lx_server_poll(lx_server* srv, long long id, int* state);
 LX_API lx_status lx_server_wait(lx_server* srv, long long id, double timeout_s, int* state);
 /* Queued requests leave the queue; running ones leave the batch at the next chunk end. */
 LX_API lx_status lx_server_cancel(lx_server* srv, long long id);
-/* Results of a DONE request: the DFT plane's flux (lx_sim_dft_flux) and max|E|^2. */
+/* Results of a DONE request: the DFT plane's flux (lx_sim_dft_flux) and max|E|^2.  They
+ * run without blocking the worker; take and release refuse a request while one runs. */
 LX_API lx_status lx_server_flux(lx_server* srv, long long id, double* flux, int nfreq);
 LX_API lx_status lx_server_max_e2(lx_server* srv, long long id, double* out);
 /* Seconds since the server was created at which the request was submitted, started
@@ -354,6 +356,8 @@ LX_API lx_status lx_server_release(lx_server* srv, long long id);
 /* Why a request FAILED ("" otherwise); valid until the request is released. */
 LX_API const char* lx_server_error(lx_server* srv, long long id);
 LX_API lx_status lx_server_stats_get(lx_server* srv, lx_server_stats* st);
+
+/* A batch is driven by one host thread at a time (the server's worker drives its own). */
 
 /* Launch all device work of the handle on this CUDA stream (cudaStream_t) instead of its
  * own.  NULL restores the handle's own stream. */

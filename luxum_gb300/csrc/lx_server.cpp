@@ -54,6 +54,7 @@ struct Request {
   int state = LX_REQ_QUEUED;
   bool cancel = false;
   int done = 0;  // steps taken
+  int readers = 0;  // client calls reading a finished request's handle outside the lock
   lx_sim* sim = nullptr;
   int dft_id = -1;
   double t_submit = -1, t_start = -1, t_end = -1;
@@ -445,23 +446,34 @@ static lx_status done_request(lx_server* srv, long long id, std::shared_ptr<Requ
   return LX_OK;
 }
 
+// Runs `read` on a finished request's handle without holding the server lock (the call may
+// wait on the GPU); take/release refuse the request meanwhile.
+template <class F>
+static lx_status read_done(lx_server* srv, long long id, F read) {
+  std::shared_ptr<Request> r;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    lx_status st = done_request(srv, id, r);
+    if (st) return st;
+    r->readers++;
+  }
+  const lx_status st = read(*r);
+  std::lock_guard<std::mutex> lk(srv->mu);
+  r->readers--;
+  return st;
+}
+
 extern "C" LX_API lx_status lx_server_flux(lx_server* srv, long long id, double* flux, int nfreq) {
   if (!srv || !flux) return sfail(LX_ERR_INVALID, "null argument");
-  std::lock_guard<std::mutex> lk(srv->mu);
-  std::shared_ptr<Request> r;
-  lx_status st = done_request(srv, id, r);
-  if (st) return st;
-  if (r->dft_id < 0) return sfail(LX_ERR_STATE, "request has no DFT plane");
-  return lx_sim_dft_flux(r->sim, r->dft_id, flux, nfreq);
+  return read_done(srv, id, [&](Request& r) {
+    if (r.dft_id < 0) return sfail(LX_ERR_STATE, "request has no DFT plane");
+    return lx_sim_dft_flux(r.sim, r.dft_id, flux, nfreq);
+  });
 }
 
 extern "C" LX_API lx_status lx_server_max_e2(lx_server* srv, long long id, double* out) {
   if (!srv || !out) return sfail(LX_ERR_INVALID, "null argument");
-  std::lock_guard<std::mutex> lk(srv->mu);
-  std::shared_ptr<Request> r;
-  lx_status st = done_request(srv, id, r);
-  if (st) return st;
-  return lx_sim_max_e2(r->sim, out);
+  return read_done(srv, id, [&](Request& r) { return lx_sim_max_e2(r.sim, out); });
 }
 
 extern "C" LX_API lx_status lx_server_times(lx_server* srv, long long id, double t[3]) {
@@ -481,6 +493,7 @@ extern "C" LX_API lx_status lx_server_take(lx_server* srv, long long id, lx_sim*
   std::shared_ptr<Request> r;
   lx_status st = done_request(srv, id, r);
   if (st) return st;
+  if (r->readers) return sfail(LX_ERR_STATE, "request is being read by another call");
   *sim = r->sim;
   r->sim = nullptr;
   srv->reqs.erase(id);
@@ -495,6 +508,7 @@ extern "C" LX_API lx_status lx_server_release(lx_server* srv, long long id) {
     auto r = find(srv, id);
     if (!r) return sfail(LX_ERR_INVALID, "no such request");
     if (!final_state(r->state)) return sfail(LX_ERR_STATE, "request is still queued or running");
+    if (r->readers) return sfail(LX_ERR_STATE, "request is being read by another call");
     s = r->sim;
     r->sim = nullptr;
     srv->reqs.erase(id);
