@@ -365,6 +365,7 @@ static void stop_writer(lx_sim* s);
 // shows in this handle's max|E|^2; only CUDA errors are returned here.
 extern "C" LX_API lx_status lx_batch_wait(lx_batch* b);
 extern "C" LX_API lx_status lx_batch_remove(lx_batch* b, lx_sim* s);
+static void batch_member_changed(lx_batch* b);
 static lx_status settle(lx_sim* s) {
   if (!s->batch) return LX_OK;
   const lx_status st = lx_batch_wait(s->batch);
@@ -971,6 +972,8 @@ extern "C" LX_API lx_status lx_sim_set_eps_box(lx_sim* s, const int lo[3], const
 
 extern "C" LX_API lx_status lx_sim_set_probes(lx_sim* s, const int* ijk, int nprobes, int cap) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  if (s->batch)
+    return fail(s, LX_ERR_STATE, "remove the handle from its batch first: batched members keep no snapshot outputs or probes");
   if (nprobes < 0 || nprobes > lx::kMaxProbes || cap < 0) return fail(s, LX_ERR_INVALID, "0..64 probes, capacity >= 0");
   CK(cudaStreamSynchronize(s->stream));
   dfree(s->d_probe_ijk, s->own);
@@ -1009,6 +1012,7 @@ extern "C" LX_API lx_status lx_sim_read_probes(lx_sim* s, double* host, size_t n
 extern "C" LX_API lx_status lx_sim_add_dft_plane(lx_sim* s, int axis, int index, int nfreq, const double* omega,
                                                  int every, int* id) {
   if (!s || !omega || !id) return fail(s, LX_ERR_INVALID, "null argument");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   if (axis < 0 || axis > 2 || (s->planar && axis == 1)) return fail(s, LX_ERR_INVALID, "axis must be 0, 1 or 2 (planar: 0 or 2)");
   const int N[3] = {s->Nx, s->Ny, s->Nz};
   if (index < 0 || index >= N[axis]) return fail(s, LX_ERR_INVALID, "plane index outside the grid");
@@ -1033,6 +1037,7 @@ extern "C" LX_API lx_status lx_sim_add_dft_plane(lx_sim* s, int axis, int index,
   s->n_h2d += nfreq * sizeof(double);
   s->dfts.push_back(d);
   *id = (int)s->dfts.size() - 1;
+  if (s->batch) batch_member_changed(s->batch);  // the batch samples the new plane from its next step
   return LX_OK;
 }
 
@@ -1162,6 +1167,8 @@ static lx_status add_output(lx_sim* s, const lx::Output& o) {
 
 extern "C" LX_API lx_status lx_sim_set_snapshots(lx_sim* s, int every, unsigned mask, lx_snapshot_fn fn, void* user) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  if (s->batch)
+    return fail(s, LX_ERR_STATE, "remove the handle from its batch first: batched members keep no snapshot outputs or probes");
   if (every < 0 || (every > 0 && !fn)) return fail(s, LX_ERR_INVALID, "every >= 0 and a callback are required");
   for (int c = 0; c < 7; c++)
     if ((mask & (1u << c)) && ext_n(s, c) == 0) return fail(s, LX_ERR_INVALID, "component absent on this grid");
@@ -1182,6 +1189,8 @@ extern "C" LX_API lx_status lx_sim_set_snapshots(lx_sim* s, int every, unsigned 
 
 extern "C" LX_API lx_status lx_sim_set_hdf5_output(lx_sim* s, int every, int first, int comp, const char* path) {
   if (!s || !path) return fail(s, LX_ERR_INVALID, "null argument");
+  if (s->batch)
+    return fail(s, LX_ERR_STATE, "remove the handle from its batch first: batched members keep no snapshot outputs or probes");
   if (every <= 0 || first < 0 || comp < 0 || comp > LX_ETOTAL || ext_n(s, comp) == 0)
     return fail(s, LX_ERR_INVALID, "bad cadence or component");
   lx::Output o;
@@ -1626,6 +1635,8 @@ struct lx_batch {
   int pending = 0;  // steps enqueued since the last wait
   std::string err;
 };
+
+static void batch_member_changed(lx_batch* b) { b->dirty = true; }
 
 static void batch_free_device(lx_batch* b) {
   for (auto& g : b->groups) {

@@ -161,3 +161,27 @@ def test_batch_autotune_leaves_members_untouched(engine):
     for m, t in zip(members, twins):
         _same(m, t)
     batch.close()
+
+
+def test_member_changes_after_joining(engine):
+    """A DFT plane added to a member after it joined is sampled from the next batch step;
+    outputs a batch cannot serve (probes, snapshots) are refused while the handle is a member."""
+    from luxum_gb300 import Batch, LuxumError
+
+    m, t = _make("planar_oblique", 1), _make("planar_oblique", 1)
+    batch = Batch(chunk=10)
+    batch.add(m)
+    batch.step(10)
+    t.step(10)
+    w = 2 * np.pi * np.linspace(3e10, 1.5e11, 5)
+    pm = m.add_dft_plane(2, 25, w, every=2)
+    pt = t.add_dft_plane(2, 25, w, every=2)
+    batch.step(25)
+    t.step(25)
+    assert np.array_equal(m.dft(pm), t.dft(pt))
+    _same(m, t)
+    with pytest.raises(LuxumError):
+        m.set_probes([[10, 0, 10]], capacity=5)
+    with pytest.raises(LuxumError):
+        m.set_snapshots(5, 1 << 1, lambda *a: None)
+    batch.close()

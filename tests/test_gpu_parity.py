@@ -230,3 +230,23 @@ def test_max_series_matches_oracle(engine, name):
         o.step(1)
         assert got_v[t] == pytest.approx(o.max_e2(), rel=1e-11, abs=1e-300), t
     assert got_v[-1] == g.max_e2()
+
+
+@pytest.mark.parametrize("shape", [(200, 7, 9), (7, 150, 9), (9, 7, 260), (40, 40, 3)])
+@pytest.mark.parametrize("pml_cells", [0, 2])
+def test_elongated_and_thin_grids(engine, shape, pml_cells):
+    """Extreme aspect ratios, slabs that cover most of an axis, and tiles that are mostly
+    outside the grid: the block-level fast path and slab tests at their edges."""
+    from luxum_gb300 import Sim
+    from oracle.oracle import OracleSim
+
+    nx, ny, nz = shape
+    kw = dict(isPlanar=0, Nx=nx, Ny=ny, Nz=nz, usePS=1, Nx_source=nx // 2, Ny_source=ny // 2, Nz_source=nz // 2 - 1,
+              amp_source=1.0, omega_source=3.0e11)
+    if pml_cells:
+        kw.update(cases.pml(pml_cells, kappa=3.0, a_max=0.0))
+    p = cases.make(**kw)
+    g, o = Sim(p), OracleSim(p, threads=4)
+    g.step(60)
+    o.step(60)
+    _compare(g, o, f"{shape} pml {pml_cells}")
