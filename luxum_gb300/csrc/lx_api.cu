@@ -936,6 +936,7 @@ static lx_status check_cb_comp(lx_sim* s, int comp, size_t n) {
 
 extern "C" LX_API lx_status lx_sim_set_cb(lx_sim* s, int comp, const double* cb, size_t n) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   lx_status st = check_cb_comp(s, comp, n);
   if (st) return st;
   if ((st = upload(s, cb, n))) return st;
@@ -946,6 +947,7 @@ extern "C" LX_API lx_status lx_sim_set_cb(lx_sim* s, int comp, const double* cb,
 
 extern "C" LX_API lx_status lx_sim_set_material(lx_sim* s, int comp, const double* F, size_t n, double scale) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   lx_status st = check_cb_comp(s, comp, n);
   if (st) return st;
   if ((st = upload(s, F, n))) return st;
@@ -956,6 +958,7 @@ extern "C" LX_API lx_status lx_sim_set_material(lx_sim* s, int comp, const doubl
 
 extern "C" LX_API lx_status lx_sim_set_eps_box(lx_sim* s, const int lo[3], const int hi[3], double eps_r) {
   if (!s || !lo || !hi) return fail(s, LX_ERR_INVALID, "null argument");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   if (!(eps_r > 0)) return fail(s, LX_ERR_INVALID, "eps_r must be > 0");
   const double val = s->k.dt / (s->k.epsilon0 * eps_r) * s->cbs_scale;
   for (int c = 0; c < 3; c++) {
@@ -1481,6 +1484,7 @@ extern "C" LX_API lx_status lx_sim_step(lx_sim* s, int nsteps) {
 
 extern "C" LX_API lx_status lx_sim_time_kernels(lx_sim* s, int nsteps, double out_ms[4]) {
   if (!s || !out_ms) return fail(s, LX_ERR_INVALID, "null argument");
+  { const lx_status st_ = settle(s); if (st_) return st_; }
   if (nsteps < 1) return fail(s, LX_ERR_INVALID, "nsteps must be >= 1");
   KernelTimer kt;
   CK(cudaEventCreate(&kt.ev[0]));
