@@ -396,6 +396,7 @@ extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
     dfree(d.d_omega, fs);
     dfree(d.d_acc, fs);
     dfree(d.d_flux, fs);
+    dfree(d.d_phase, fs);
   }
   if (s->own) {
     cudaStreamSynchronize(s->own);
@@ -1036,6 +1037,7 @@ extern "C" LX_API lx_status lx_sim_add_dft_plane(lx_sim* s, int axis, int index,
   CK(cudaMemcpyAsync(d.d_omega, omega, nfreq * sizeof(double), cudaMemcpyHostToDevice, s->own));
   CK(cudaMallocAsync(&d.d_acc, d.n_acc * sizeof(double), s->own));
   CK(cudaMemsetAsync(d.d_acc, 0, d.n_acc * sizeof(double), s->own));
+  CK(cudaMallocAsync(&d.d_phase, 4 * lx::kMaxDftFreq * sizeof(double), s->own));
   CK(cudaStreamSynchronize(s->own));
   s->n_h2d += nfreq * sizeof(double);
   s->dfts.push_back(d);
@@ -1426,14 +1428,14 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
       std::memset(&dp, 0, sizeof dp);
       dp.axis = d.axis; dp.index = d.index; dp.na = d.na; dp.nb = d.nb; dp.Ny = s->Ny; dp.Nzp = s->Nzp;
       dp.nfreq = d.nfreq; dp.t = t; dp.dt = s->k.dt; dp.weight = (double)d.every;
-      dp.omega = d.d_omega; dp.acc = d.d_acc; dp.hmul = 1.0 / s->hscale;
+      dp.omega = d.d_omega; dp.acc = d.d_acc; dp.phase = d.d_phase; dp.hmul = 1.0 / s->hscale;
       T* f4[4];
       for (int q = 0; q < 4; q++) {
         f4[q] = pf[d.comps[q]];
         for (int a = 0; a < 3; a++) dp.ext[q][a] = s->ext[d.comps[q]][a];
       }
       CK(lx::launch_dft<T>(dp, f4, s->stream));
-      s->n_kernels++;
+      s->n_kernels += 2;  // phase factors, accumulation
     }
     if (s->nprobes > 0 && s->probe_rows < s->probe_cap) {
       prb.row = s->probe_rows++;
@@ -1768,7 +1770,7 @@ static lx_status batch_rebuild(lx_batch* b) {
       std::memset(&dp, 0, sizeof dp);
       dp.axis = d.axis; dp.index = d.index; dp.na = d.na; dp.nb = d.nb; dp.Ny = s->Ny; dp.Nzp = s->Nzp;
       dp.nfreq = d.nfreq; dp.dt = s->k.dt; dp.weight = (double)d.every; dp.every_ = d.every;
-      dp.omega = d.d_omega; dp.acc = d.d_acc; dp.sim = q; dp.hmul = 1.0 / s->hscale;
+      dp.omega = d.d_omega; dp.acc = d.d_acc; dp.phase = d.d_phase; dp.sim = q; dp.hmul = 1.0 / s->hscale;
       for (int c = 0; c < 4; c++) {
         dp.f[c] = pf[d.comps[c]];
         for (int a = 0; a < 3; a++) dp.ext[c][a] = s->ext[d.comps[c]][a];
@@ -1859,7 +1861,7 @@ static lx_status batch_enqueue(lx_batch* b, long long step0, int nsteps) {
     const long long bs = step0 + q;
     for (auto& cl : b->dft)
       if (bs % cl.every == cl.phase)
-        BCK(lx::launch_dft_batch<T>(cl.d_planes, cl.d_map, cl.nblocks, b->d_ts, q, b->stream));
+        BCK(lx::launch_dft_batch<T>(cl.d_planes, cl.d_map, cl.nplanes, cl.nblocks, b->d_ts, q, b->stream));
   }
   if (nsteps > 0) BCK(lx::launch_tick(b->d_ts, n, nsteps, b->stream));
   return LX_OK;

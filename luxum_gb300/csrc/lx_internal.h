@@ -139,6 +139,7 @@ struct DftParams {
   double hmul;            // 1/hscale for the two H components
   int every_;             // batched launches: sampling cadence
   const double* omega;    // device [nfreq]
+  double* phase;          // device [4][kMaxDftFreq]: cos, sin (E), cos, sin (H) of this sample
   double* acc;            // device [nfreq][4][na*nb][2]
 };
 

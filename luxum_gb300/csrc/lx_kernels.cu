@@ -900,18 +900,43 @@ __global__ void probe_kernel(const ProbeParams pp, const T* f0, const T* f1, con
   out[(long long)pp.row * pp.nprobes * 6 + q] = v;
 }
 
-// Running DFT of the four tangential components on one plane.  Each block evaluates the
-// phase factors of every frequency once into shared memory; each thread owns one
-// (component, cell) and updates its nfreq complex accumulators (coalesced along the cell).
-template <class T>
-__device__ __forceinline__ void dft_body(const DftParams& d, const int t, const T* f0, const T* f1, const T* f2,
-                                         const T* f3, const int lb) {
-  __shared__ double cs[2][kMaxDftFreq], sn[2][kMaxDftFreq];
+// Phase factors of one sample of a DFT plane: cos/sin of omega*(t+1)*dt for the E
+// components (sampled after the E update) and of omega*(t+0.5)*dt for the H components,
+// formed once per plane and sample (the accumulating blocks then only read them).
+__device__ __forceinline__ void dft_phase_body(const DftParams& d, const int t) {
   for (int f = threadIdx.x; f < d.nfreq; f += blockDim.x) {
     const double pe = __dmul_rn(d.omega[f], __dmul_rn((double)(t + 1), d.dt));
     const double ph = __dmul_rn(d.omega[f], __dmul_rn((double)t + 0.5, d.dt));
-    sincos(pe, &sn[0][f], &cs[0][f]);
-    sincos(ph, &sn[1][f], &cs[1][f]);
+    double se, ce, sh, ch;
+    sincos(pe, &se, &ce);
+    sincos(ph, &sh, &ch);
+    d.phase[f] = ce;
+    d.phase[kMaxDftFreq + f] = se;
+    d.phase[2 * kMaxDftFreq + f] = ch;
+    d.phase[3 * kMaxDftFreq + f] = sh;
+  }
+}
+
+__global__ void dft_phase_kernel(const DftParams d) { dft_phase_body(d, d.t); }
+
+// Batched: one block per plane of a sampling class.
+__global__ void dft_phase_batch_kernel(const DftParams* __restrict__ ds, const int* __restrict__ ts, int k) {
+  const DftParams& d = ds[blockIdx.x];
+  dft_phase_body(d, ts[d.sim] + k);
+}
+
+// Running DFT of the four tangential components on one plane.  Each thread owns one
+// (component, cell) and updates its nfreq complex accumulators (coalesced along the cell),
+// four frequencies at a time with their loads issued before their stores.
+template <class T>
+__device__ __forceinline__ void dft_body(const DftParams& d, const T* f0, const T* f1, const T* f2, const T* f3,
+                                         const int lb) {
+  __shared__ double cs[2][kMaxDftFreq], sn[2][kMaxDftFreq];
+  for (int f = threadIdx.x; f < d.nfreq; f += blockDim.x) {
+    cs[0][f] = d.phase[f];
+    sn[0][f] = d.phase[kMaxDftFreq + f];
+    cs[1][f] = d.phase[2 * kMaxDftFreq + f];
+    sn[1][f] = d.phase[3 * kMaxDftFreq + f];
   }
   __syncthreads();
   const long long ncell = (long long)d.na * d.nb;
@@ -934,22 +959,35 @@ __device__ __forceinline__ void dft_body(const DftParams& d, const int t, const 
   if (comp >= 2 && d.hmul != 1.0) v = __dmul_rn(v, d.hmul);
   v = __dmul_rn(v, d.weight);
   const int w = comp < 2 ? 0 : 1;
-  double2* acc = reinterpret_cast<double2*>(d.acc);
-  for (int fq = 0; fq < d.nfreq; ++fq) {
-    double2 x = acc[((long long)fq * 4 + comp) * ncell + cell];
+  double2* acc = reinterpret_cast<double2*>(d.acc) + (long long)comp * ncell + cell;
+  const long long stride = 4 * ncell;  // from one frequency to the next
+  int fq = 0;
+  for (; fq + 4 <= d.nfreq; fq += 4) {
+    double2 x[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) x[r] = acc[(fq + r) * stride];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      x[r].x = fma(v, cs[w][fq + r], x[r].x);
+      x[r].y = fma(-v, sn[w][fq + r], x[r].y);
+      acc[(fq + r) * stride] = x[r];
+    }
+  }
+  for (; fq < d.nfreq; ++fq) {
+    double2 x = acc[fq * stride];
     x.x = fma(v, cs[w][fq], x.x);
     x.y = fma(-v, sn[w][fq], x.y);
-    acc[((long long)fq * 4 + comp) * ncell + cell] = x;
+    acc[fq * stride] = x;
   }
 }
 
 template <class T>
 __global__ void dft_kernel(const DftParams d, const T* f0, const T* f1, const T* f2, const T* f3) {
-  dft_body<T>(d, d.t, f0, f1, f2, f3, blockIdx.x);
+  dft_body<T>(d, f0, f1, f2, f3, blockIdx.x);
 }
 
-// Batched DFT planes: a flat launch over the planes sampled at this step; bfirst[q] is the
-// first block of plane q (each block serves one plane, so its phase table is per plane).
+// Batched DFT planes: a flat launch over the planes sampled at this step; map gives each
+// block its plane and its block within the plane.
 template <class T>
 __global__ void dft_batch_kernel(const DftParams* __restrict__ ds, const int2* __restrict__ map, const int* __restrict__ ts,
                                  int k) {
@@ -957,7 +995,7 @@ __global__ void dft_batch_kernel(const DftParams* __restrict__ ds, const int2* _
   const DftParams& d = ds[bm.x];
   const int t = ts[d.sim] + k;
   if (t % d.every_ != 0) return;
-  dft_body<T>(d, t, (const T*)d.f[0], (const T*)d.f[1], (const T*)d.f[2], (const T*)d.f[3], bm.y);
+  dft_body<T>(d, (const T*)d.f[0], (const T*)d.f[1], (const T*)d.f[2], (const T*)d.f[3], bm.y);
 }
 
 // Net flux of a DFT plane per frequency: partial sums over fixed chunks of 1024 cells, then
@@ -1075,6 +1113,7 @@ cudaError_t launch_probes(const ProbeParams& pp, T* const f[6], double* out, cud
 template <class T>
 cudaError_t launch_dft(const DftParams& d, T* const f[4], cudaStream_t s) {
   const long long n = 4LL * d.na * d.nb;
+  dft_phase_kernel<<<1, 128, 0, s>>>(d);
   dft_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, f[0], f[1], f[2], f[3]);
   return cudaGetLastError();
 }
@@ -1153,8 +1192,10 @@ cudaError_t launch_tick(int* ts, int n, int steps, cudaStream_t s) {
 }
 
 template <class T>
-cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nblocks, const int* ts, int k, cudaStream_t s) {
+cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nplanes, int nblocks, const int* ts, int k,
+                             cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
+  dft_phase_batch_kernel<<<nplanes, 128, 0, s>>>(ds, ts, k);
   dft_batch_kernel<T><<<nblocks, 256, 0, s>>>(ds, map, ts, k);
   return cudaGetLastError();
 }
@@ -1178,7 +1219,7 @@ cudaError_t launch_dft_flux(const double* acc, int nfreq, long long ncell, doubl
                                                 cudaStream_t);                                                     \
   template cudaError_t launch_batch_step<T, C>(const StepParams<T, C>*, const int4*, int, bool, bool, int, bool,     \
                                                cudaStream_t);                                                          \
-  template cudaError_t launch_dft_batch<T>(const DftParams*, const int2*, int, const int*, int, cudaStream_t);
+  template cudaError_t launch_dft_batch<T>(const DftParams*, const int2*, int, int, const int*, int, cudaStream_t);
 LX_INST(double, double)
 LX_INST(float, float)
 LX_INST(__half, float)

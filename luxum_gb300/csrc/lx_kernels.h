@@ -43,7 +43,8 @@ cudaError_t launch_prologue_batch(const PrologueParams* pps, const int* ts, int 
                                   cudaStream_t s);
 cudaError_t launch_tick(int* ts, int n, int steps, cudaStream_t s);
 template <class T>
-cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nblocks, const int* ts, int k, cudaStream_t s);
+cudaError_t launch_dft_batch(const DftParams* ds, const int2* map, int nplanes, int nblocks, const int* ts, int k,
+                             cudaStream_t s);
 cudaError_t launch_dft_flux(const double* acc, int nfreq, long long ncell, double* part, double dA, double* out,
                             cudaStream_t s);
 

@@ -42,6 +42,7 @@ struct DftPlane {
   double* d_omega = nullptr;
   double* d_acc = nullptr;
   double* d_flux = nullptr;  // flux result + per-chunk partial sums
+  double* d_phase = nullptr;  // phase factors of the current sample (4 x kMaxDftFreq)
   size_t n_acc = 0;  // doubles
 };
 
