@@ -381,8 +381,10 @@ extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
   cudaStream_t fs = s->own;
   for (int c = 0; c < 3; c++) {
     dfree(s->E[c], fs); dfree(s->H[c], fs); dfree(s->Cbs[c], fs);
+    dfree(s->E1[c], fs); dfree(s->H1[c], fs);
     for (int q = 0; q < 6; q++) dfree(s->prof[c][q], fs);
     for (int q = 0; q < 2; q++) { dfree(s->psiH[c][q], fs); dfree(s->psiE[c][q], fs); }
+    for (int q = 0; q < 2; q++) { dfree(s->psiH1[c][q], fs); dfree(s->psiE1[c][q], fs); }
   }
   dfree(s->tab, fs); dfree(s->d_max, fs); dfree(s->d_series, fs); dfree(s->etotal, fs); dfree(s->xfer, fs);
   dfree(s->d_probe_ijk, fs); dfree(s->d_probe, fs);
@@ -423,11 +425,13 @@ static lx_status create_typed(lx_sim* s) {
   for (int c = 0; c < 3; c++) {
     if (s->planar && c != 1) continue;
     if ((st = alloc_zero(s, &s->E[c], fb))) return st;
+    if (s->sweep && (st = alloc_zero(s, &s->E1[c], fb))) return st;
     if ((st = alloc_zero(s, &s->Cbs[c], s->ncell * sizeof(C)))) return st;
   }
   for (int c = 0; c < 3; c++) {
     if (s->planar && c == 1) continue;
     if ((st = alloc_zero(s, &s->H[c], fb))) return st;
+    if (s->sweep && (st = alloc_zero(s, &s->H1[c], fb))) return st;
   }
   // Cb = dt/epsilon0 (two_dim.cc:81, two_dim_pml.cc:116, three_dim.cc:54)
   s->cb0 = K.dt / K.epsilon0;
@@ -475,10 +479,12 @@ static lx_status create_typed(lx_sim* s) {
         if (useH) {
           s->psiH_n[c][part] = psi_size(axH[c][part]);
           if ((st = alloc_zero(s, &s->psiH[c][part], s->psiH_n[c][part] * sizeof(C)))) return st;
+          if (s->sweep && (st = alloc_zero(s, &s->psiH1[c][part], s->psiH_n[c][part] * sizeof(C)))) return st;
         }
         if (useE) {
           s->psiE_n[c][part] = psi_size(axE[c][part]);
           if ((st = alloc_zero(s, &s->psiE[c][part], s->psiE_n[c][part] * sizeof(C)))) return st;
+          if (s->sweep && (st = alloc_zero(s, &s->psiE1[c][part], s->psiE_n[c][part] * sizeof(C)))) return st;
         }
       }
   }
@@ -509,6 +515,13 @@ static void setup_host(lx_sim* s, const lx_params* p) {
   s->Nzp = (s->Nz + per - 1) / per * per;
   s->ncell = (size_t)s->Nx * s->Ny * s->Nzp;
   compute_extents(s);
+  // Planar handles with float compute step in one sweep over two state buffers; FP64 is bound
+  // by the FP64 pipe, where the sweep's recomputed halo would only add work.  LUXUM_TWO_SWEEP=1
+  // in the environment keeps new handles on the in-place two-sweep kernels (A/B checks).
+  {
+    const char* two = std::getenv("LUXUM_TWO_SWEEP");
+    s->sweep = s->planar && p->precision != LX_PREC_FP64 && !(two && two[0] == '1');
+  }
 
   // maxwell::maxwell maxwell.cc:60-148
   lx::Consts& K = s->k;
@@ -586,6 +599,7 @@ extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
   }
   s->stream = s->own;
   st = (s->csize == 8) ? create_typed<double>(s) : create_typed<float>(s);
+  s->pp = s->sweep;
   if (st == LX_OK) {
     e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) st = fail(s, LX_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
@@ -618,8 +632,8 @@ extern "C" LX_API lx_status lx_params_device_bytes(const lx_params* p, size_t* b
   lx_sim tmp;
   setup_host(&tmp, p);
   size_t b = 0;
-  const int nE = tmp.planar ? 1 : 3, nH = tmp.planar ? 2 : 3;
-  b += (size_t)(nE + nH) * tmp.ncell * tmp.tsize + (size_t)nE * tmp.ncell * tmp.csize;
+  const int nE = tmp.planar ? 1 : 3, nH = tmp.planar ? 2 : 3, nbuf = tmp.sweep ? 2 : 1;
+  b += (size_t)nbuf * (nE + nH) * tmp.ncell * tmp.tsize + (size_t)nE * tmp.ncell * tmp.csize;
   if (tmp.pml) {
     for (int a = 0; a < 3; a++) {
       if (tmp.planar && a == 1) continue;
@@ -632,7 +646,7 @@ extern "C" LX_API lx_status lx_params_device_bytes(const lx_params* p, size_t* b
       const Slab& sl = tmp.slab[a];
       const size_t plane = a == 0 ? (size_t)tmp.Ny * tmp.Nzp : (a == 1 ? (size_t)tmp.Nx * tmp.Nzp : (size_t)tmp.Nx * tmp.Ny);
       // psi arrays whose derivative runs along this axis: 4 in 3-D (2 H + 2 E), 2 in planar
-      b += (size_t)(tmp.planar ? 2 : 4) * sl.n * plane * tmp.csize;
+      b += (size_t)nbuf * (tmp.planar ? 2 : 4) * sl.n * plane * tmp.csize;
     }
   }
   if (tmp.tfsf) {
@@ -649,11 +663,13 @@ extern "C" LX_API lx_status lx_sim_reset(lx_sim* s) {
   if (st) return st;
   const size_t fb = s->ncell * s->tsize;
   for (int c = 0; c < 3; c++) {
-    if (s->E[c]) CK(cudaMemsetAsync(s->E[c], 0, fb, s->stream));
-    if (s->H[c]) CK(cudaMemsetAsync(s->H[c], 0, fb, s->stream));
+    for (void* f : {s->E[c], s->H[c], s->E1[c], s->H1[c]})
+      if (f) CK(cudaMemsetAsync(f, 0, fb, s->stream));
     for (int q = 0; q < 2; q++) {
-      if (s->psiH[c][q]) CK(cudaMemsetAsync(s->psiH[c][q], 0, s->psiH_n[c][q] * s->csize, s->stream));
-      if (s->psiE[c][q]) CK(cudaMemsetAsync(s->psiE[c][q], 0, s->psiE_n[c][q] * s->csize, s->stream));
+      for (void* f : {s->psiH[c][q], s->psiH1[c][q]})
+        if (f) CK(cudaMemsetAsync(f, 0, s->psiH_n[c][q] * s->csize, s->stream));
+      for (void* f : {s->psiE[c][q], s->psiE1[c][q]})
+        if (f) CK(cudaMemsetAsync(f, 0, s->psiE_n[c][q] * s->csize, s->stream));
     }
   }
   if (s->etotal) CK(cudaMemsetAsync(s->etotal, 0, s->ncell * s->csize, s->stream));
@@ -677,11 +693,47 @@ static lx_status ensure_xfer(lx_sim* s) {
   return LX_OK;
 }
 
-static void* comp_ptr(lx_sim* s, int comp) {
-  if (comp >= LX_EX && comp <= LX_EZ) return s->E[comp];
-  if (comp >= LX_HX && comp <= LX_HZ) return s->H[comp - 3];
-  if (comp == LX_ETOTAL) return s->etotal;
+// The buffer holding the current state (buffer t & 1 in ping-pong mode, else 0), and the other.
+static bool odd_state(const lx_sim* s) { return s->pp && (s->t & 1); }
+
+static void* comp_ptr(lx_sim* s, int comp, bool other = false) {
+  const bool b1 = odd_state(s) != other;
+  if (comp >= LX_EX && comp <= LX_EZ) return b1 ? s->E1[comp] : s->E[comp];
+  if (comp >= LX_HX && comp <= LX_HZ) return b1 ? s->H1[comp - 3] : s->H[comp - 3];
+  if (comp == LX_ETOTAL) return other ? nullptr : s->etotal;
   return nullptr;
+}
+
+static void* psi_ptr(lx_sim* s, bool h, int a, int q, bool other = false) {
+  const bool b1 = odd_state(s) != other;
+  if (h) return b1 ? s->psiH1[a][q] : s->psiH[a][q];
+  return b1 ? s->psiE1[a][q] : s->psiE[a][q];
+}
+
+// Switches a single-sweep handle between ping-pong mode (stepped alone: the state after t
+// steps in buffer t & 1) and in-place mode (batched: the state in buffer 0).  At odd t the
+// state moves between the buffers, one device copy of the fields and psi.
+static lx_status set_pp(lx_sim* s, bool on) {
+  if (!s->sweep || (s->pp != 0) == on) return LX_OK;
+  if (s->t & 1) {
+    const size_t fb = s->ncell * s->tsize;
+    auto move = [&](void* b0, void* b1, size_t bytes) -> lx_status {
+      if (!b0 || !bytes) return LX_OK;
+      CK(cudaMemcpyAsync(on ? b1 : b0, on ? b0 : b1, bytes, cudaMemcpyDeviceToDevice, s->stream));
+      return LX_OK;
+    };
+    lx_status st;
+    for (int c = 0; c < 3; c++) {
+      if ((st = move(s->E[c], s->E1[c], fb))) return st;
+      if ((st = move(s->H[c], s->H1[c], fb))) return st;
+      for (int q = 0; q < 2; q++) {
+        if ((st = move(s->psiH[c][q], s->psiH1[c][q], s->psiH_n[c][q] * s->csize))) return st;
+        if ((st = move(s->psiE[c][q], s->psiE1[c][q], s->psiE_n[c][q] * s->csize))) return st;
+      }
+    }
+  }
+  s->pp = on;
+  return LX_OK;
 }
 
 static lx_status gather(lx_sim* s, int comp, double* dst) {
@@ -757,6 +809,10 @@ extern "C" LX_API lx_status lx_sim_write_field(lx_sim* s, int comp, const double
   if (st) return st;
   const bool hcomp = comp >= LX_HX && comp <= LX_HZ;
   if ((st = scatter(s, comp, comp_ptr(s, comp), false, hcomp && s->hscale != 1.0 ? 1 : 0, s->hscale, 0.0))) return st;
+  // single-sweep handles: the other buffer too, so that the values stay the state whichever
+  // buffer the step count selects (a checkpoint load sets the step count afterwards)
+  if (s->sweep && (st = scatter(s, comp, comp_ptr(s, comp, true), false, hcomp && s->hscale != 1.0 ? 1 : 0, s->hscale, 0.0)))
+    return st;
   CK(cudaStreamSynchronize(s->stream));
   return LX_OK;
 }
@@ -851,7 +907,7 @@ extern "C" LX_API lx_status lx_sim_save(lx_sim* s, const char* path) {
       for (int h = 0; h < 2; h++) {
         const size_t n = h ? s->psiH_n[a][q] : s->psiE_n[a][q];
         if (!n) continue;
-        if ((st = raw_to_host(s, h ? s->psiH[a][q] : s->psiE[a][q], n, host))) return st;
+        if ((st = raw_to_host(s, psi_ptr(s, h, a, q), n, host))) return st;
         const int ext[3] = {1, 1, (int)n};
         if ((st = put(std::string(h ? "psiH_" : "psiE_") + char('0' + a) + char('0' + q), host, ext))) return st;
       }
@@ -916,7 +972,8 @@ extern "C" LX_API lx_status lx_sim_load(lx_sim* s, const char* path) {
         const size_t n = h ? s->psiH_n[a][q] : s->psiE_n[a][q];
         if (!n) continue;
         if ((st = get(std::string(h ? "psiH_" : "psiE_") + char('0' + a) + char('0' + q), n))) return st;
-        if ((st = raw_to_device(s, h ? s->psiH[a][q] : s->psiE[a][q], v))) return st;
+        if ((st = raw_to_device(s, psi_ptr(s, h, a, q), v))) return st;
+        if (s->sweep && (st = raw_to_device(s, psi_ptr(s, h, a, q, true), v))) return st;
       }
   for (size_t d = 0; d < s->dfts.size(); d++) {
     if ((st = get("dft_" + std::to_string(d), s->dfts[d].n_acc))) return st;
@@ -1282,6 +1339,8 @@ static lx::StepParams<T, C> step_params(lx_sim* s) {
   for (int c = 0; c < 3; c++) {
     p.E[c] = (T*)s->E[c];
     p.H[c] = (T*)s->H[c];
+    p.E1[c] = (T*)s->E1[c];
+    p.H1[c] = (T*)s->H1[c];
     p.Cbs[c] = (const C*)s->Cbs[c];
   }
   const double Db = s->k.dt / s->k.mew0;  // Db arrays = dt/mew0 (two_dim_pml.cc:117, three_dim_pml.cc:130-132)
@@ -1305,6 +1364,8 @@ static lx::StepParams<T, C> step_params(lx_sim* s) {
     for (int q = 0; q < 2; q++) {
       p.psiH[c][q] = (C*)s->psiH[c][q];
       p.psiE[c][q] = (C*)s->psiE[c][q];
+      p.psiH1[c][q] = (C*)s->psiH1[c][q];
+      p.psiE1[c][q] = (C*)s->psiE1[c][q];
       p.setsH[c][q] = s->setsH[c][q];
       p.setsE[c][q] = s->setsE[c][q];
     }
@@ -1322,6 +1383,19 @@ static lx::StepParams<T, C> step_params(lx_sim* s) {
       if (e.active) { p.planesE[e.axis][0] = e.plane[0]; p.planesE[e.axis][1] = e.plane[1]; }
     }
   return p;
+}
+
+// The parameter block of a single-sweep step that reads buffer 1 and writes buffer 0.
+template <class T, class C>
+static void swap_buffers(lx::StepParams<T, C>& p) {
+  for (int c = 0; c < 3; c++) {
+    std::swap(p.E[c], p.E1[c]);
+    std::swap(p.H[c], p.H1[c]);
+    for (int q = 0; q < 2; q++) {
+      std::swap(p.psiH[c][q], p.psiH1[c][q]);
+      std::swap(p.psiE[c][q], p.psiE1[c][q]);
+    }
+  }
 }
 
 // Optional per-launch timing of run_steps (lx_sim_time_kernels).
@@ -1351,6 +1425,7 @@ static lx::PrologueParams make_prologue(lx_sim* s) {
   pp.src_kind = s->src_kind;
   pp.src_idx = s->src_idx;
   pp.src_field = s->planar ? s->E[1] : s->E[2];
+  pp.src_field1 = s->pp ? (s->planar ? s->E1[1] : s->E1[2]) : nullptr;  // ping-pong mode: used at odd t
   pp.src_amp_i = (int)s->p.amp_source;  // maxwell.cc:142-143 store them in int members
   pp.src_omega_i = (int)s->p.omega_source;
   pp.src_amp = s->p.amp_source;
@@ -1363,9 +1438,20 @@ static lx::PrologueParams make_prologue(lx_sim* s) {
 
 template <class T, class C>
 static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
+  if (!s->batch) {  // stepped alone: single-sweep handles take the ping-pong kernel
+    const lx_status st = set_pp(s, true);
+    if (st) return st;
+  }
   lx::StepParams<T, C> sp = step_params<T, C>(s);
   lx::PrologueParams pp = make_prologue(s);
-  T* pf[6] = {(T*)s->E[0], (T*)s->E[1], (T*)s->E[2], (T*)s->H[0], (T*)s->H[1], (T*)s->H[2]};
+  T* pf[6];  // the components after the current step (buffer (t+1) & 1 in ping-pong mode)
+  auto post_step = [&](int t) {
+    const bool b1 = s->pp && ((t + 1) & 1);
+    for (int c = 0; c < 3; c++) {
+      pf[c] = (T*)(b1 ? s->E1[c] : s->E[c]);
+      pf[3 + c] = (T*)(b1 ? s->H1[c] : s->H[c]);
+    }
+  };
   lx::ProbeParams prb;
   std::memset(&prb, 0, sizeof prb);
   prb.nprobes = s->nprobes;
@@ -1413,15 +1499,30 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
       if ((st = toc(0))) return st;
       s->n_kernels++;
     }
-    if ((st = tic())) return st;
-    CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, true, s->stream));
-    if ((st = toc(1))) return st;
     sp.max_slot = mon ? slot : nullptr;
     sp.etotal = (snap & (1u << LX_ETOTAL)) ? (C*)s->etotal : nullptr;
-    if ((st = tic())) return st;
-    CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, false, s->stream));
-    if ((st = toc(2))) return st;
-    s->n_kernels += 2;
+    bool swept = false;
+    if constexpr (sizeof(C) == 4) {
+      if (s->pp) {  // one launch: H and E of the step, state t & 1 -> (t+1) & 1
+        lx::StepParams<T, C> sw = sp;
+        if (t & 1) swap_buffers(sw);
+        if ((st = tic())) return st;
+        CK(lx::launch_step_sweep2<T, C>(sw, s->uniform, s->stream));
+        if ((st = toc(1))) return st;
+        s->n_kernels += 1;
+        swept = true;
+      }
+    }
+    if (!swept) {
+      if ((st = tic())) return st;
+      CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, true, s->stream));
+      if ((st = toc(1))) return st;
+      if ((st = tic())) return st;
+      CK(lx::launch_step<T, C>(sp, s->planar, s->uniform, false, s->stream));
+      if ((st = toc(2))) return st;
+      s->n_kernels += 2;
+    }
+    post_step(t);
     for (auto& d : s->dfts) {
       if (t % d.every != 0) continue;
       lx::DftParams dp;
@@ -1561,15 +1662,15 @@ extern "C" LX_API lx_status lx_sim_info(const lx_sim* s, lx_info* info) {
   info->cells = (size_t)s->Nx * s->Ny * s->Nz;
   size_t b = 0;
   for (int c = 0; c < 3; c++) {
-    if (s->E[c]) b += s->ncell * s->tsize;
-    if (s->H[c]) b += s->ncell * s->tsize;
+    for (void* f : {s->E[c], s->H[c], s->E1[c], s->H1[c]})
+      if (f) b += s->ncell * s->tsize;
     if (s->Cbs[c]) b += s->ncell * s->csize;
     for (int q = 0; q < 2; q++) {
       info->psi_h_entries += s->psiH_n[c][q];
       info->psi_e_entries += s->psiE_n[c][q];
     }
   }
-  b += (info->psi_h_entries + info->psi_e_entries) * s->csize;
+  b += (s->sweep ? 2 : 1) * (info->psi_h_entries + info->psi_e_entries) * s->csize;
   if (s->etotal) b += s->ncell * s->csize;
   b += s->xfer_cap * sizeof(double) + (size_t)s->tab_total * s->csize;
   for (auto& sl : s->slots) b += sl.cap * sizeof(double);
@@ -1726,6 +1827,7 @@ extern "C" LX_API lx_status lx_batch_add(lx_batch* b, lx_sim* s) {
   if (!s->outputs.empty() || s->nprobes > 0 || s->d_series)
     return bfail(b, LX_ERR_UNSUPPORTED, "batched members cannot have snapshot outputs, probes or a max series");
   if ((st = lx_sim_sync(s))) return st;
+  if ((st = set_pp(s, false))) return st;  // batches update their members in place
   b->prec = s->prec;
   b->sims.push_back(s);
   s->batch = b;

@@ -82,6 +82,7 @@ struct PrologueParams {
   int src_kind;       // -1 none, 0 hard CW, 1 additive pulse
   long long src_idx;  // linear index in the padded layout
   void* src_field;    // Ez (3D) or Ey (planar pulse)
+  void* src_field1;   // its buffer 1 on single-sweep handles (used at odd t), else null
   int src_amp_i, src_omega_i;
   double src_amp, src_omega, src_t0, src_tw;
   int prec;           // storage precision of src_field
@@ -119,7 +120,42 @@ struct StepParams {
   // monitor / |E|^2 snapshot (E kernel)
   unsigned long long* max_slot;  // atomicMax of the bit pattern of max|E|^2 (non-negative)
   C* etotal;                     // when non-null, |E|^2 into the Ez-shaped array (3D)
+  // Single-sweep handles keep two copies of the state: after t steps it lives in buffer t & 1
+  // (buffer 0 = E, H, psiH, psiE above; buffer 1 here, null for handles updated in place).
+  T* E1[3];
+  T* H1[3];
+  C* psiH1[3][2];
+  C* psiE1[3][2];
 };
+
+// Whether a block's tile [i0,i0+ni) x [j0,j0+nj) x [k0,k0+nk) meets any TF/SF plane of the
+// given plane lists; blocks that do not skip every per-cell plane test.
+__host__ __device__ inline bool tile_meets_planes(const int (&pl)[3][2], int i0, int ni, int j0, int nj, int k0, int nk) {
+  bool t = false;
+  for (int q = 0; q < 2; ++q) {
+    t |= (unsigned)(pl[0][q] - i0) < (unsigned)ni;
+    t |= (unsigned)(pl[1][q] - j0) < (unsigned)nj;
+    t |= (unsigned)(pl[2][q] - k0) < (unsigned)nk;
+  }
+  return t;
+}
+
+// Whether a tile [i0,i0+ni) x [j0,j0+nj) x [k0,k0+nk) lies where every component of both
+// half steps updates (every index in [1, N-2]) and no CPML slab reaches.  Such tiles (most
+// of a grid) take the cell code with every per-cell condition decided at compile time.
+__host__ __device__ inline bool axis_free(const Slab& s, int a, int n) { return s.n == 0 || (a >= s.lo && a + n <= s.hi0); }
+__host__ __device__ inline bool tile_is_interior(const Slab (&sl)[3], bool pml, int Nx, int Ny, int Nz, int i0, int ni,
+                                                 int j0, int nj, int k0, int nk) {
+  if (i0 < 1 || i0 + ni > Nx - 1 || j0 < 1 || j0 + nj > Ny - 1 || k0 < 1 || k0 + nk > Nz - 1) return false;
+  return !pml || (axis_free(sl[0], i0, ni) && axis_free(sl[1], j0, nj) && axis_free(sl[2], k0, nk));
+}
+
+// The same for a planar tile [i0,i0+ni) x [k0,k0+nk) (no y axis).
+__host__ __device__ inline bool tile_is_interior_2d(const Slab (&sl)[3], bool pml, int Nx, int Nz, int i0, int ni,
+                                                    int k0, int nk) {
+  if (i0 < 1 || i0 + ni > Nx - 1 || k0 < 1 || k0 + nk > Nz - 1) return false;
+  return !pml || (axis_free(sl[0], i0, ni) && axis_free(sl[2], k0, nk));
+}
 
 // Probe sampling of one step row.
 struct ProbeParams {

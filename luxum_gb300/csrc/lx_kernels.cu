@@ -44,6 +44,11 @@ __device__ __forceinline__ void st<__half, float>(__half* p, float v) {
 
 __device__ __forceinline__ double fmaC(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fmaC(float a, float b, float c) { return fmaf(a, b, c); }
+// A rounded product that is never contracted into a neighbouring add: the 1/d factors of
+// non-uniform spacing.  Contraction decisions differ between kernels, and the single-sweep
+// and two-sweep planar kernels must give the same bits (the oracle does not contract).
+__device__ __forceinline__ double mulC(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mulC(float a, float b) { return __fmul_rn(a, b); }
 
 // ------------------------------------------------------------------ TF/SF
 
@@ -65,36 +70,6 @@ __device__ __forceinline__ void tfsf_apply(const PatchSet& ps, const C* tab, int
   const int off = ui * ps.stride[0] + uj * ps.stride[1] + uk * ps.stride[2];
   if (h0) d = d + tab[ps.tab + off];
   if (h1) d = d + tab[ps.tab + ps.plane_len + off];
-}
-
-// Whether a block's tile [i0,i0+ni) x [j0,j0+nj) x [k0,k0+nk) meets any TF/SF plane of the
-// given plane lists; blocks that do not skip every per-cell plane test.
-__device__ __forceinline__ bool tile_meets_planes(const int (&pl)[3][2], int i0, int ni, int j0, int nj, int k0, int nk) {
-  bool t = false;
-#pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    t |= (unsigned)(pl[0][q] - i0) < (unsigned)ni;
-    t |= (unsigned)(pl[1][q] - j0) < (unsigned)nj;
-    t |= (unsigned)(pl[2][q] - k0) < (unsigned)nk;
-  }
-  return t;
-}
-
-// Whether a tile [i0,i0+ni) x [j0,j0+nj) x [k0,k0+nk) lies where every component of both
-// half steps updates (every index in [1, N-2]) and no CPML slab reaches.  Such tiles (most
-// of a grid) take the cell code with every per-cell condition decided at compile time.
-__device__ __forceinline__ bool axis_free(const Slab& s, int a, int n) { return s.n == 0 || (a >= s.lo && a + n <= s.hi0); }
-__device__ __forceinline__ bool tile_is_interior(const Slab (&sl)[3], bool pml, int Nx, int Ny, int Nz, int i0, int ni,
-                                                 int j0, int nj, int k0, int nk) {
-  if (i0 < 1 || i0 + ni > Nx - 1 || j0 < 1 || j0 + nj > Ny - 1 || k0 < 1 || k0 + nk > Nz - 1) return false;
-  return !pml || (axis_free(sl[0], i0, ni) && axis_free(sl[1], j0, nj) && axis_free(sl[2], k0, nk));
-}
-
-// The same for a planar tile [i0,i0+ni) x [k0,k0+nk) (no y axis).
-__device__ __forceinline__ bool tile_is_interior_2d(const Slab (&sl)[3], bool pml, int Nx, int Nz, int i0, int ni,
-                                                    int k0, int nk) {
-  if (i0 < 1 || i0 + ni > Nx - 1 || k0 < 1 || k0 + nk > Nz - 1) return false;
-  return !pml || (axis_free(sl[0], i0, ni) && axis_free(sl[2], k0, nk));
 }
 
 // psi = b*psi + c*curl; returns curl/kappa + psi (reference: three_dim_pml.cc:186-188).
@@ -151,20 +126,21 @@ __device__ __forceinline__ void prologue_body(const PrologueParams& p, const int
                                               const int gstride) {
   if (gid == 0) {
     if (p.max_slot) *p.max_slot = 0ull;
+    void* const src_field = ((t & 1) && p.src_field1) ? p.src_field1 : p.src_field;  // the state step t reads
     if (p.src_kind == 0) {
       // amp_source*sin(omega_source*t*dt), int members (maxwell.h:203,206; three_dim_pml.cc:163)
       const int wt = (int)((unsigned)p.src_omega_i * (unsigned)t);
       const double v = (double)p.src_amp_i * sin((double)wt * p.dt);
-      if (p.prec == 0) ((double*)p.src_field)[p.src_idx] = v;
-      else if (p.prec == 1) ((float*)p.src_field)[p.src_idx] = (float)v;
-      else ((__half*)p.src_field)[p.src_idx] = __double2half(v);
+      if (p.prec == 0) ((double*)src_field)[p.src_idx] = v;
+      else if (p.prec == 1) ((float*)src_field)[p.src_idx] = (float)v;
+      else ((__half*)src_field)[p.src_idx] = __double2half(v);
     } else if (p.src_kind == 1) {
       const double u = (t - p.src_t0) / p.src_tw;
       const double v = p.src_amp * exp(-(u * u)) * sin(p.src_omega * t * p.dt);
-      if (p.prec == 0) ((double*)p.src_field)[p.src_idx] += v;
-      else if (p.prec == 1) ((float*)p.src_field)[p.src_idx] += (float)v;
+      if (p.prec == 0) ((double*)src_field)[p.src_idx] += v;
+      else if (p.prec == 1) ((float*)src_field)[p.src_idx] += (float)v;
       else {
-        __half* f = (__half*)p.src_field;
+        __half* f = (__half*)src_field;
         f[p.src_idx] = __float2half_rn(__half2float(f[p.src_idx]) + (float)v);
       }
     }
@@ -325,7 +301,7 @@ __device__ __forceinline__ void h_apply(const StepParams<T, C>& p, const int i, 
   // Hx: i < Nx, j < Ny-1, k < Nz-1; part 1 = dEz/dy (y profile), part 2 = dEy/dz (z profile)
   if (ux) {
     C d1 = ez_j - ez, d2 = ey_k - ey;
-    if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
+    if (!UNI) { d1 = mulC(d1, p.rd[1]); d2 = mulC(d2, p.rd[2]); }
     if (tf) {
       tfsf_apply<C>(p.setsH[0][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsH[0][1], p.tab, i, j, k, d2);
@@ -337,7 +313,7 @@ __device__ __forceinline__ void h_apply(const StepParams<T, C>& p, const int i, 
   // Hy: i < Nx-1, j < Ny, k < Nz-1; part 1 = dEx/dz (z), part 2 = dEz/dx (x)
   if (uy) {
     C d1 = ex_k - ex, d2 = ez_i - ez;
-    if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
+    if (!UNI) { d1 = mulC(d1, p.rd[2]); d2 = mulC(d2, p.rd[0]); }
     if (tf) {
       tfsf_apply<C>(p.setsH[1][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsH[1][1], p.tab, i, j, k, d2);
@@ -349,7 +325,7 @@ __device__ __forceinline__ void h_apply(const StepParams<T, C>& p, const int i, 
   // Hz: i < Nx-1, j < Ny-1, k < Nz; part 1 = dEy/dx (x), part 2 = dEx/dy (y)
   if (uz) {
     C d1 = ey_i - ey, d2 = ex_j - ex;
-    if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
+    if (!UNI) { d1 = mulC(d1, p.rd[0]); d2 = mulC(d2, p.rd[1]); }
     if (tf) {
       tfsf_apply<C>(p.setsH[2][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsH[2][1], p.tab, i, j, k, d2);
@@ -453,7 +429,7 @@ __device__ __forceinline__ typename MaxBits<C>::type e_apply(const StepParams<T,
   // Ex: i < Nx-1, j in [1,Ny-2], k in [1,Nz-2]; part 1 = dHz/dy (y), part 2 = dHy/dz (z)
   if (ux) {
     C d1 = hz - hz_j, d2 = hy - hy_k;
-    if (!UNI) { d1 *= p.rd[1]; d2 *= p.rd[2]; }
+    if (!UNI) { d1 = mulC(d1, p.rd[1]); d2 = mulC(d2, p.rd[2]); }
     if (tf) {
       tfsf_apply<C>(p.setsE[0][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsE[0][1], p.tab, i, j, k, d2);
@@ -465,7 +441,7 @@ __device__ __forceinline__ typename MaxBits<C>::type e_apply(const StepParams<T,
   // Ey: i in [1,Nx-2], j < Ny-1, k in [1,Nz-2]; part 1 = dHx/dz (z), part 2 = dHz/dx (x)
   if (uy) {
     C d1 = hx - hx_k, d2 = hz - hz_i;
-    if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
+    if (!UNI) { d1 = mulC(d1, p.rd[2]); d2 = mulC(d2, p.rd[0]); }
     if (tf) {
       tfsf_apply<C>(p.setsE[1][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsE[1][1], p.tab, i, j, k, d2);
@@ -477,7 +453,7 @@ __device__ __forceinline__ typename MaxBits<C>::type e_apply(const StepParams<T,
   // Ez: i in [1,Nx-2], j in [1,Ny-2], k < Nz-1; part 1 = dHy/dx (x), part 2 = dHx/dy (y)
   if (uz) {
     C d1 = hy - hy_i, d2 = hx - hx_j;
-    if (!UNI) { d1 *= p.rd[0]; d2 *= p.rd[1]; }
+    if (!UNI) { d1 = mulC(d1, p.rd[0]); d2 = mulC(d2, p.rd[1]); }
     if (tf) {
       tfsf_apply<C>(p.setsE[2][0], p.tab, i, j, k, d1);
       tfsf_apply<C>(p.setsE[2][1], p.tab, i, j, k, d2);
@@ -562,7 +538,7 @@ __device__ __forceinline__ void h2_apply(const StepParams<T, C>& p, const int i,
   // Hx: k < Nz-1; Hx -= Db*(-curl2/kappa - psi2), curl2 = dEy/dz (z profile)
   if (ux) {
     C d2 = ey_k - ey;
-    if (!UNI) d2 *= p.rd[2];
+    if (!UNI) d2 = mulC(d2, p.rd[2]);
     if (tf) tfsf_apply<C>(p.setsH[0][1], p.tab, i, 0, k, d2);
     if (!FAST && p.pml) {
       const int sz = slab_index(p.slab[2], k);
@@ -573,7 +549,7 @@ __device__ __forceinline__ void h2_apply(const StepParams<T, C>& p, const int i,
   // Hz: i < Nx-1; Hz -= Db*(curl1/kappa + psi1), curl1 = dEy/dx (x profile)
   if (uz) {
     C d1 = ey_i - ey;
-    if (!UNI) d1 *= p.rd[0];
+    if (!UNI) d1 = mulC(d1, p.rd[0]);
     if (tf) tfsf_apply<C>(p.setsH[2][0], p.tab, i, 0, k, d1);
     if (!FAST && p.pml) {
       const int sx = slab_index(p.slab[0], i);
@@ -639,7 +615,7 @@ __device__ __forceinline__ typename MaxBits<C>::type e2_apply(const StepParams<T
   if (FAST || v.u) {
     C d1 = v.hx - v.hx_k;  // dHx/dz (z profile)
     C d2 = v.hz - v.hz_i;  // dHz/dx (x profile)
-    if (!UNI) { d1 *= p.rd[2]; d2 *= p.rd[0]; }
+    if (!UNI) { d1 = mulC(d1, p.rd[2]); d2 = mulC(d2, p.rd[0]); }
     if (tf) {
       tfsf_apply<C>(p.setsE[1][0], p.tab, i, 0, k, d1);
       tfsf_apply<C>(p.setsE[1][1], p.tab, i, 0, k, d2);
@@ -676,6 +652,197 @@ __global__ void __launch_bounds__(256) e_kernel_2d(const StepParams<T, C> p) {
     else mbits = e_cell_2d<T, C, UNI, MON>(p, i, k, tf);
   }
   if (MON && p.max_slot) block_max_atomic(mbits, p.max_slot);
+}
+
+// ------------------------------------------------------------------ single-sweep planar step
+
+// Planar step in one sweep, for float compute.  The two-sweep kernels above move 40 bytes per
+// FP32 cell and step (H sweep: Ey read, Hx and Hz read and written; E sweep: Hx, Hz and Cb read,
+// Ey read and written); one sweep moves the compulsory 28 (Ey, Hx, Hz and Cb read once, Ey, Hx
+// and Hz written once).  A warp owns 32 z columns and R consecutive x rows and walks the rows in
+// order.  At row i it forms H(i): Hx from Ey(i,k+1) (a shuffle) and Hz from Ey(i+1,k), the next
+// row's value, which it keeps for the next iteration.  Then it forms E(i) from H(i), the Hx of
+// column k-1 (a shuffle) and the Hz of row i-1, kept from the previous iteration.  Two values
+// belong to other warps and are recomputed from the old state with the same code as their
+// owners': Hz(i0-1) before the first row, and lane 0's Hx(i,k0-1).  State n is read from one
+// buffer and state n+1 written to the other, so no warp sees a neighbour's new values, and every
+// cell of the run is written (the cells a half step does not update keep their old value).  H
+// enters E as stored (FP16 storage rounds it first), so the step matches the two-sweep kernels
+// bit for bit.
+
+// A computed value as a later load of the stored value returns it.
+template <class T, class C>
+__device__ __forceinline__ C stored(C v) {
+  return static_cast<C>(static_cast<T>(v));
+}
+template <>
+__device__ __forceinline__ float stored<__half, float>(float v) {
+  return __half2float(__float2half_rn(v));
+}
+
+// New Hx of planar cell (i,k), k < Nz-1: the arithmetic of h2_apply (two_dim_pml.cc:149-152).
+// A null psi_out recomputes a neighbour's value and leaves its psi to the owner.
+template <class T, class C, bool UNI, bool FAST>
+__device__ __forceinline__ C hx2_value(const StepParams<T, C>& p, const C* psi_in, C* psi_out, int i, int k, C ey,
+                                       C ey_k, C hx, bool tf) {
+  C d2 = ey_k - ey;
+  if (!UNI) d2 = mulC(d2, p.rd[2]);
+  if (!FAST && tf) tfsf_apply<C>(p.setsH[0][1], p.tab, i, 0, k, d2);
+  if (!FAST && p.pml) {
+    const int sz = slab_index(p.slab[2], k);
+    if (sz >= 0) {
+      const long long q = (long long)i * p.slab[2].n + sz;
+      const C ps = fmaC(p.bH[2][k], psi_in[q], p.cH[2][k] * d2);
+      if (psi_out) psi_out[q] = ps;
+      d2 = fmaC(d2, p.rkH[2][k], ps);
+    }
+  }
+  return fmaC(p.Dbs, d2, hx);
+}
+
+// New Hz of planar cell (i,k), i < Nx-1 (two_dim_pml.cc:155-158).
+template <class T, class C, bool UNI, bool FAST>
+__device__ __forceinline__ C hz2_value(const StepParams<T, C>& p, const C* psi_in, C* psi_out, int i, int k, C ey,
+                                       C ey_i, C hz, bool tf) {
+  C d1 = ey_i - ey;
+  if (!UNI) d1 = mulC(d1, p.rd[0]);
+  if (!FAST && tf) tfsf_apply<C>(p.setsH[2][0], p.tab, i, 0, k, d1);
+  if (!FAST && p.pml) {
+    const int sx = slab_index(p.slab[0], i);
+    if (sx >= 0) {
+      const long long q = (long long)sx * p.Nzp + k;
+      const C ps = fmaC(p.bH[0][i], psi_in[q], p.cH[0][i] * d1);
+      if (psi_out) psi_out[q] = ps;
+      d1 = fmaC(d1, p.rkH[0][i], ps);
+    }
+  }
+  return fmaC(-p.Dbs, d1, hz);
+}
+
+// New Ey of planar cell (i,k), i and k in [1, N-2] (two_dim_pml.cc:164-176): e2_apply's arithmetic.
+template <class T, class C, bool UNI, bool FAST>
+__device__ __forceinline__ C ey2_value(const StepParams<T, C>& p, const C* pz_in, C* pz_out, const C* px_in, C* px_out,
+                                       int i, int k, C ey, C hx, C hx_k, C hz, C hz_i, C cb, bool tf) {
+  C d1 = hx - hx_k;  // dHx/dz (z profile)
+  C d2 = hz - hz_i;  // dHz/dx (x profile)
+  if (!UNI) { d1 = mulC(d1, p.rd[2]); d2 = mulC(d2, p.rd[0]); }
+  if (!FAST && tf) {
+    tfsf_apply<C>(p.setsE[1][0], p.tab, i, 0, k, d1);
+    tfsf_apply<C>(p.setsE[1][1], p.tab, i, 0, k, d2);
+  }
+  if (!FAST && p.pml) {
+    const int sz = slab_index(p.slab[2], k), sx = slab_index(p.slab[0], i);
+    if (sz >= 0) {
+      const long long q = (long long)i * p.slab[2].n + sz;
+      const C ps = fmaC(p.bE[2][k], pz_in[q], p.cE[2][k] * d1);
+      pz_out[q] = ps;
+      d1 = fmaC(d1, p.rkE[2][k], ps);
+    }
+    if (sx >= 0) {
+      const long long q = (long long)sx * p.Nzp + k;
+      const C ps = fmaC(p.bE[0][i], px_in[q], p.cE[0][i] * d2);
+      px_out[q] = ps;
+      d2 = fmaC(d2, p.rkE[0][i], ps);
+    }
+  }
+  return fmaC(cb, d1 - d2, ey);
+}
+
+// One warp's rows [i0, i1) of the 32 columns from k0; returns the bit pattern of its largest
+// Ey^2 (the max over the whole Ey array, two_dim_pml.cc:181).
+// The parameter block names the buffer read in E, H, psiH, psiE and the one written in E1,
+// H1, psiH1, psiE1 (the host swaps them on odd steps).
+template <class T, class C, bool UNI, bool FAST>
+__device__ __forceinline__ typename MaxBits<C>::type step2_rows(const StepParams<T, C>& p, const int i0, const int i1,
+                                                                const int k0, const bool tfH, const bool tfE) {
+  const int lane = threadIdx.x;
+  const int k = k0 + lane;
+  const int Nx = p.Nx, Nz = p.Nz;
+  const T* eyi = p.E[1];
+  T* eyo = p.E1[1];
+  const T* hxi = p.H[0];
+  T* hxo = p.H1[0];
+  const T* hzi = p.H[2];
+  T* hzo = p.H1[2];
+  const C* qhx = p.psiH[0][1];  // Hx, z part
+  C* qhxo = p.psiH1[0][1];
+  const C* qhz = p.psiH[2][0];  // Hz, x part
+  C* qhzo = p.psiH1[2][0];
+  const C* qez = p.psiE[1][0];  // Ey, z part
+  C* qezo = p.psiE1[1][0];
+  const C* qex = p.psiE[1][1];  // Ey, x part
+  C* qexo = p.psiE1[1][1];
+  const bool kin = FAST || k < Nz;
+  const bool ux = FAST || k < Nz - 1;
+  const bool ke = FAST || (k >= 1 && k < Nz - 1);
+  const long long si = p.si;
+  long long c = (long long)i0 * si + k;
+  C ey = kin ? ld<T, C>(eyi + c) : C(0);
+  C hz_p = C(0);  // new Hz of the row above
+  if (i0 >= 1) {
+    const C eym = kin ? ld<T, C>(eyi + c - si) : C(0);
+    const C hzm = kin ? ld<T, C>(hzi + c - si) : C(0);
+    hz_p = stored<T, C>(hz2_value<T, C, UNI, FAST>(p, qhz, nullptr, i0 - 1, k, eym, ey, hzm, tfH));
+  }
+  typename MaxBits<C>::type m = 0;
+#pragma unroll 1
+  for (int i = i0; i < i1; ++i, c += si) {
+    const bool nx = FAST || i + 1 < Nx;
+    const bool ue = ke && (FAST || (i >= 1 && i < Nx - 1));
+    const C eyn = (kin && nx) ? ld<T, C>(eyi + c + si) : C(0);
+    const C hx = kin ? ld<T, C>(hxi + c) : C(0);
+    const C hz = kin ? ld<T, C>(hzi + c) : C(0);
+    const C cb = (kin && ue) ? p.Cbs[1][c] : C(0);
+    C ey_k = __shfl_down_sync(0xffffffffu, ey, 1);
+    if (lane == 31) ey_k = (FAST || k + 1 < Nz) ? ld<T, C>(eyi + c + 1) : C(0);
+    C hxh = C(0), eyh = C(0);  // lane 0: Hx and Ey of column k0-1
+    if (lane == 0 && k0 >= 1) {
+      hxh = ld<T, C>(hxi + c - 1);
+      eyh = ld<T, C>(eyi + c - 1);
+    }
+    const C hxn = (kin && ux) ? stored<T, C>(hx2_value<T, C, UNI, FAST>(p, qhx, qhxo, i, k, ey, ey_k, hx, tfH)) : hx;
+    const C hzn = (kin && nx) ? stored<T, C>(hz2_value<T, C, UNI, FAST>(p, qhz, qhzo, i, k, ey, eyn, hz, tfH)) : hz;
+    C hx_k = __shfl_up_sync(0xffffffffu, hxn, 1);
+    if (lane == 0)
+      hx_k = k0 >= 1 ? stored<T, C>(hx2_value<T, C, UNI, FAST>(p, qhx, nullptr, i, k0 - 1, eyh, ey, hxh, tfH)) : C(0);
+    const C eyw = (kin && ue) ? ey2_value<T, C, UNI, FAST>(p, qez, qezo, qex, qexo, i, k, ey, hxn, hx_k, hzn, hz_p, cb, tfE)
+                              : ey;
+    if (kin) {
+      st<T, C>(hxo + c, hxn);
+      st<T, C>(hzo + c, hzn);
+      st<T, C>(eyo + c, eyw);
+      const typename MaxBits<C>::type b = MaxBits<C>::of(eyw * eyw);
+      m = b > m ? b : m;
+    }
+    hz_p = hzn;
+    ey = eyn;
+  }
+  return m;
+}
+
+// A warp's run with its TF/SF and interior tests: H is formed on rows [i0-1, i1) and columns
+// [k0-1, k0+32), E on rows [i0, i1) and columns [k0, k0+32).
+template <class T, class C, bool UNI>
+__device__ __forceinline__ typename MaxBits<C>::type step2_warp(const StepParams<T, C>& p, const int i0, const int i1,
+                                                                const int k0) {
+  const bool tfH = p.tfsf && tile_meets_planes(p.planesH, i0 - 1, i1 - i0 + 1, 0, 1, k0 - 1, 34);
+  const bool tfE = p.tfsf && tile_meets_planes(p.planesE, i0, i1 - i0, 0, 1, k0, 32);
+  if (!tfH && !tfE && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, i0 - 1, i1 - i0 + 2, k0 - 1, 34))
+    return step2_rows<T, C, UNI, true>(p, i0, i1, k0, false, false);
+  return step2_rows<T, C, UNI, false>(p, i0, i1, k0, tfH, tfE);
+}
+
+// Register cap of the single-sweep kernel: 6 blocks of 256 per SM (40 registers, no spills).
+constexpr int kSweepMinBlocks = 6;
+
+// One simulation: a block is 32 z columns x 8 warps of R rows.
+template <class T, class C, bool UNI, int R>
+__global__ void __launch_bounds__(256, kSweepMinBlocks) step_kernel_2d(const StepParams<T, C> p) {
+  const int k0 = blockIdx.x * 32;
+  const int i0 = (blockIdx.y * 8 + threadIdx.y) * R;
+  typename MaxBits<C>::type m = 0;
+  if (i0 < p.Nx) m = step2_warp<T, C, UNI>(p, i0, min(i0 + R, p.Nx), k0);
+  if (p.max_slot) block_max_atomic(m, p.max_slot);
 }
 
 // ------------------------------------------------------------------ batched update kernels
@@ -1078,6 +1245,26 @@ cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bo
   return cudaGetLastError();
 }
 
+template <class T, class C>
+cudaError_t launch_step_sweep2(const StepParams<T, C>& p, bool uniform, cudaStream_t s) {
+  // rows per warp: 16 where that still gives every SM 32 warps, fewer on small grids
+  const long long cols = (p.Nz + 31) / 32;
+  int R = 16;
+  while (R > 2 && cols * ((p.Nx + R - 1) / R) < 152LL * 32) R /= 2;
+  const dim3 block(32, 8), grid((unsigned)cols, (unsigned)((p.Nx + 8 * R - 1) / (8 * R)));
+  switch (R * 2 + (uniform ? 1 : 0)) {
+    case 32: step_kernel_2d<T, C, false, 16><<<grid, block, 0, s>>>(p); break;
+    case 33: step_kernel_2d<T, C, true, 16><<<grid, block, 0, s>>>(p); break;
+    case 16: step_kernel_2d<T, C, false, 8><<<grid, block, 0, s>>>(p); break;
+    case 17: step_kernel_2d<T, C, true, 8><<<grid, block, 0, s>>>(p); break;
+    case 8: step_kernel_2d<T, C, false, 4><<<grid, block, 0, s>>>(p); break;
+    case 9: step_kernel_2d<T, C, true, 4><<<grid, block, 0, s>>>(p); break;
+    case 4: step_kernel_2d<T, C, false, 2><<<grid, block, 0, s>>>(p); break;
+    default: step_kernel_2d<T, C, true, 2><<<grid, block, 0, s>>>(p); break;
+  }
+  return cudaGetLastError();
+}
+
 template <class T>
 cudaError_t launch_gather(const T* src, double* dst, const int ext[3], int Ny, int Nzp, double mul, cudaStream_t s) {
   const long long n = (long long)ext[0] * ext[1] * ext[2];
@@ -1223,6 +1410,8 @@ cudaError_t launch_dft_flux(const double* acc, int nfreq, long long ncell, doubl
 LX_INST(double, double)
 LX_INST(float, float)
 LX_INST(__half, float)
+template cudaError_t launch_step_sweep2<float, float>(const StepParams<float, float>&, bool, cudaStream_t);
+template cudaError_t launch_step_sweep2<__half, float>(const StepParams<__half, float>&, bool, cudaStream_t);
 template cudaError_t launch_prologue<double>(const PrologueParams&, cudaStream_t);
 template cudaError_t launch_prologue<float>(const PrologueParams&, cudaStream_t);
 template cudaError_t launch_prologue_batch<double>(const PrologueParams*, const int*, int, int, int, cudaStream_t);

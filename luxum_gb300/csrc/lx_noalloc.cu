@@ -105,7 +105,9 @@ extern "C" LX_API lx_status lx_sim_read_field_noalloc(lx_sim* s, int comp, doubl
     const lx_status st = lx_batch_wait(s->batch);
     if (st && st != LX_ERR_BLOWUP) return st;
   }
-  const void* src = comp <= LX_EZ ? s->E[comp] : (comp <= LX_HZ ? s->H[comp - 3] : s->etotal);
+  const bool b1 = s->pp && (s->t & 1);  // ping-pong mode: the state after t steps is in buffer t & 1
+  const void* src = comp <= LX_EZ ? (b1 ? s->E1[comp] : s->E[comp])
+                                  : (comp <= LX_HZ ? (b1 ? s->H1[comp - 3] : s->H[comp - 3]) : s->etotal);
   if (!src) return bad(LX_ERR_STATE, comp == LX_ETOTAL ? "|E|^2 is only kept when a snapshot asks for it" : "component absent");
   double* staging = nullptr;
   cudaError_t e = staging_address(&staging);

@@ -82,6 +82,16 @@ struct lx_sim {
   void* prof[3][6] = {};  // per axis: bE cE rkE bH cH rkH (compute precision)
   void* psiH[3][2] = {};
   void* psiE[3][2] = {};
+  // Single-sweep handles (planar, float compute) keep a second copy of the state.  Stepped
+  // alone they run in ping-pong mode (pp): after t steps the state lives in buffer t & 1
+  // (buffer 0 = E, H, psiH, psiE above, buffer 1 here).  In a batch they are updated in place
+  // in buffer 0 (pp = 0); set_pp moves the state when the mode changes.
+  int sweep = 0;
+  int pp = 0;
+  void* E1[3] = {};
+  void* H1[3] = {};
+  void* psiH1[3][2] = {};
+  void* psiE1[3][2] = {};
   size_t psiH_n[3][2] = {}, psiE_n[3][2] = {};
   lx::Slab slab[3] = {};
   void* tab = nullptr;

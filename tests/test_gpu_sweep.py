@@ -1,0 +1,169 @@
+"""Single-sweep planar step against the two-sweep kernels.
+
+Planar handles with float compute (FP32 and FP16 storage) form H and E of a step in one
+launch over two state buffers: state n is read from one and state n+1 written to the other.
+Handles created while LUXUM_TWO_SWEEP=1 is set use the in-place two-sweep kernels instead.
+Both must give the same fields, DFT accumulators, probe series and max|E|^2 series, bit for
+bit: at odd and even step counts, through a checkpoint written at an odd step, and across
+joining and leaving a batch (batches update their members in place).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+OMEGA = 2 * np.pi * np.linspace(3e10, 1.5e11, 5)
+
+
+def _big(precision, uniform=True):
+    """A planar grid large enough for full 16-row warps and interior blocks: CPML 16, TF/SF
+    box, a pulsed point source, a dielectric block."""
+    kw = dict(isPlanar=1, Nx=300, Ny=1, Nz=520, **cases.pw((1, 0, 0), (0, 1, 0), ((24, 275), (0, 0), (24, 495))),
+              **cases.pml(16), usePS=1, source_kind=1, Nx_source=150, Nz_source=260, amp_source=1.0,
+              omega_source=2.0e11, src_t0=15.0, src_tw=6.0, precision=precision)
+    if not uniform:
+        kw["dz"] = 0.8e-3
+    return cases.make(**kw), [((120, 0, 200), (180, 1, 330), 4.0)]
+
+
+def _small(name, precision):
+    p, _, boxes = cases.build(name)
+    p.precision = precision
+    return p, boxes
+
+
+def _sim(p, boxes, dft=True):
+    from luxum_gb300 import Sim
+
+    s = Sim(p)
+    for lo, hi, eps in boxes:
+        s.set_eps_box(lo, hi, eps)
+    if dft:
+        s.add_dft_plane(0, p.Nx // 3, OMEGA)
+        s.add_dft_plane(2, p.Nz // 2, OMEGA, every=3)  # z-normal: its first sampled component (Ex) is absent
+    return s
+
+
+def _pair(p, boxes, dft=True):
+    """(single-sweep handle, two-sweep handle) of the same parameters."""
+    os.environ.pop("LUXUM_TWO_SWEEP", None)
+    a = _sim(p, boxes, dft)
+    os.environ["LUXUM_TWO_SWEEP"] = "1"
+    try:
+        b = _sim(p, boxes, dft)
+    finally:
+        del os.environ["LUXUM_TWO_SWEEP"]
+    # the single-sweep handle holds a second copy of the fields
+    assert a.info()["device_bytes"] > b.info()["device_bytes"]
+    return a, b
+
+
+def _same(a, b):
+    assert a.t == b.t
+    for c in (1, 3, 5):  # Ey, Hx, Hz
+        assert np.array_equal(a.field(c), b.field(c)), (a.t, c)
+    for plane in getattr(a, "_dft", {}):
+        assert np.array_equal(a.dft(plane), b.dft(plane)), a.t
+    assert a.max_e2() == b.max_e2()
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("name", ["planar_pml_axis", "planar_oblique", "planar_pml_std_oblique"])
+def test_sweep_equals_two_sweep_small(engine, name, precision):
+    a, b = _pair(*_small(name, precision))
+    for n in (1, 36, 1, 2, 17):  # odd and even step counts
+        a.step(n)
+        b.step(n)
+        _same(a, b)
+    assert np.isfinite(a.max_e2()) and a.max_e2() > 0
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("uniform", [True, False])
+def test_sweep_equals_two_sweep_large(engine, precision, uniform):
+    p, boxes = _big(precision, uniform)
+    a, b = _pair(p, boxes)
+    ijk = np.array([[150, 0, 260], [30, 0, 40], [200, 0, 500], [298, 0, 518]], dtype=np.int32)
+    for s in (a, b):
+        s.set_probes(ijk, 200)
+        s.set_max_series(200)
+    a.step(61)
+    b.step(61)
+    _same(a, b)
+    a.step(40)
+    b.step(40)
+    _same(a, b)
+    assert np.array_equal(a.probes(), b.probes())
+    ta, va = a.max_series()
+    tb, vb = b.max_series()
+    assert np.array_equal(ta, tb) and np.array_equal(va, vb)
+
+
+def test_sweep_write_field_and_reset(engine):
+    """Values written at an odd step are the state whichever buffer the next step reads."""
+    p, boxes = _big(1)
+    a, b = _pair(p, boxes, dft=False)
+    a.step(11)
+    b.step(11)
+    rng = np.random.default_rng(7)
+    for c in (1, 3, 5):
+        v = rng.standard_normal(a.shape(c)) * 1e-3
+        a.set_field(c, v)
+        b.set_field(c, v)
+    a.step(9)
+    b.step(9)
+    _same(a, b)
+    a.reset()
+    b.reset()
+    a.step(3)
+    b.step(3)
+    _same(a, b)
+
+
+def test_sweep_checkpoint_at_odd_step(engine, tmp_path):
+    p, boxes = _big(1)
+    a, b = _pair(p, boxes)
+    a.step(33)
+    b.step(33)
+    path = str(tmp_path / "odd.h5")
+    a.save(path)
+    c = _sim(p, boxes)
+    c.load(path)
+    assert c.t == 33
+    for s in (a, b, c):
+        s.step(24)
+    _same(a, b)
+    _same(c, b)
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_sweep_handles_in_a_batch(engine, precision):
+    """Batches update their members in place: a single-sweep handle that joins at an odd step
+    moves its state into buffer 0, and back into buffer t & 1 when it steps alone again."""
+    from luxum_gb300 import Batch
+
+    specs = [_small("planar_pml_axis", precision), _small("planar_oblique", precision), _big(precision)]
+    pairs = [_pair(p, boxes) for p, boxes in specs]
+    for k, (a, b) in enumerate(pairs):  # ping-pong steps before joining, odd and even counts
+        a.step(3 + k)
+        b.step(3 + k)
+    batch = Batch(chunk=10)
+    for a, _ in pairs:
+        batch.add(a)
+    pairs[1][0].step(3)  # a member steps alone between batch steps
+    pairs[1][1].step(3)
+    batch.step(36)  # graph replays and direct steps
+    for _, b in pairs:
+        b.step(36)
+    for a, b in pairs:
+        _same(a, b)
+    batch.remove(pairs[0][0])  # leaves at an odd step count and steps alone again
+    assert pairs[0][0].t % 2 == 1
+    for a, b in pairs:
+        a.step(6)
+        b.step(6)
+        _same(a, b)
