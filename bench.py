@@ -54,14 +54,40 @@ def workload_params(precision: int = 0, n: int = N):
                   precision=precision, n_threads=os.cpu_count() or 1, monitor_every=1)
 
 
-def profile_case(n: int, steps: int, precision: int) -> None:
+def planar_params(precision: int, n: int):
+    """The 512^2 planar layout at n^2: CPML 20 cells, TF/SF box 10 cells inside it, Ey
+    polarisation at normal incidence from the left."""
+    from luxum_gb300 import params
+
+    lo, hi = 30, n - 31
+    return params(isPlanar=1, Nx=n, Ny=1, Nz=n, dx=1e-3, dy=1e-3, dz=1e-3, S=0.5, num_timesteps=STEPS,
+                  usePW=1, kx_pw=1.0, ky_pw=0.0, kz_pw=0.0, Ex_pw=0.0, Ey_pw=1.0, Ez_pw=0.0, off_pw=26.0,
+                  x1_pw=lo, x2_pw=hi, y1_pw=0, y2_pw=0, z1_pw=lo, z2_pw=hi, usePML=1, d_pml=20e-3, sigma=0.65,
+                  sigma_m=3.0, kappa=5.0, a_max=0.05, a_m=1.0, precision=precision, n_threads=1, monitor_every=1)
+
+
+def profile_case(n: int, steps: int, precision: int, planar: bool = False) -> None:
     """Small case for ncu captures: the workload at n^3 (n=192: 0.6 GB resident at FP64,
-    above the 129 MB L2), `steps` time steps after 60 untimed ones (wave inside the box)."""
+    above the 129 MB L2), `steps` time steps after 60 untimed ones (wave inside the box).
+    planar: the 512^2 layout at n^2 with its centred eps_r 10.89 square (n=4096: 0.47 GB at
+    FP32 with the second state buffer)."""
     import __graft_entry__
 
     __graft_entry__.build()
     from luxum_gb300 import Sim
 
+    if planar:
+        sim = Sim(planar_params(precision, n))
+        a, b = n * 224 // 512, n * 288 // 512
+        sim.set_eps_box((a, 0, a), (b, 1, b), 10.89)
+        sim.step(60)
+        kt = sim.time_kernels(steps)  # CUDA events around each launch (meaningless under ncu)
+        ms = kt["h_update"] + kt["e_update"]
+        print(json.dumps({"profile_case": n, "planar": 1, "steps": 60 + steps, "precision": precision,
+                          "update_ms_per_step": ms, "gcell_per_s": n * n / ms * 1e-6, "max_e2": sim.max_e2(),
+                          "two_sweep": os.environ.get("LUXUM_TWO_SWEEP") == "1"}))
+        sim.close()
+        return
     sim = Sim(workload_params(precision, n))
     a, b = n * 104 // 256, n * 152 // 256
     sim.set_eps_box((a, a, a), (b, b, b), 6.0)
@@ -591,6 +617,7 @@ def main():
                     help="run the N^3 profiling case instead of the benchmark (for ncu)")
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--precision", type=int, default=0, help="profiling case precision: 0 fp64, 1 fp32, 2 fp16")
+    ap.add_argument("--planar", action="store_true", help="profiling case: the planar layout at N^2")
     ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "batch3d", "serve", "phc"],
                     help="drop-in: the headline 256^3 FP64 workload; batch: 256 uneven planar simulations")
     ap.add_argument("--batch-sims", type=int, default=256)
@@ -611,7 +638,7 @@ def main():
     if args.config == "phc":
         return bench_phc(args)
     if args.profile:
-        return profile_case(args.profile, args.profile_steps, args.precision)
+        return profile_case(args.profile, args.profile_steps, args.precision, args.planar)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

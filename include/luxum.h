@@ -366,7 +366,9 @@ LX_API lx_status lx_sim_set_stream(lx_sim* sim, void* cuda_stream);
 /* Instrumented pass: runs nsteps steps with a CUDA event around every launch on the
  * handle's stream and returns the mean device time per launch in milliseconds of
  * out_ms[0] step prologue, [1] H-update kernel, [2] E-update kernel, [3] probe kernel
- * (0 when that kernel did not run).  The steps advance the simulation like lx_sim_step. */
+ * (0 when that kernel did not run).  Planar handles with FP32 or FP16 storage step H and E
+ * in one launch, reported in [1] (and 0 in [2]).  The steps advance the simulation like
+ * lx_sim_step. */
 LX_API lx_status lx_sim_time_kernels(lx_sim* sim, int nsteps, double out_ms[4]);
 
 /* Sizes of a handle's device state (engine feature). */
