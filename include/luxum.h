@@ -252,7 +252,10 @@ LX_API lx_status lx_hdf5_read(const char* path, const char* dataset, double* out
 /* ---- batches: many independent simulations stepped together (engine feature) ----
  * Member handles keep their own device state; each step runs one prologue launch, one H and
  * one E launch per group of members sharing (planar, uniform spacing) over a tile table of
- * all of them, one launch for every member's DFT planes and a step-counter tick.  Chunks of
+ * all of them, one launch for every member's DFT planes and a step-counter tick.  3-D
+ * members of 2^18 cells or more instead take one H and one E launch each, spread over four
+ * streams so that they overlap.  Members are updated in place (planar FP32/FP16 handles
+ * move their state into their first buffer on joining).  Chunks of
  * steps are captured once as a CUDA graph and replayed.  All members share one precision;
  * members may not have snapshot outputs or probes (use lx_sim_step for those).  max|E|^2
  * is monitored every step.  A handle belongs to at most one batch; lx_sim_step on a member
@@ -274,8 +277,8 @@ LX_API lx_status lx_batch_step(lx_batch* b, int nsteps);
 LX_API lx_status lx_batch_step_async(lx_batch* b, int nsteps);
 LX_API lx_status lx_batch_wait(lx_batch* b);
 /* Tile shape of the batched update kernels: cells each thread walks along x, for planar
- * members (rows 8 apart) and for 3-D members (planes); each 1, 2, 4 or 8 (defaults 8, 8).
- * Results do not depend on it, only speed. */
+ * members (rows 8 apart) and for 3-D members below 2^18 cells (planes); each 1, 2, 4 or 8
+ * (defaults 8, 8).  Results do not depend on it, only speed. */
 LX_API lx_status lx_batch_set_march(lx_batch* b, int planar_rows, int planes_3d);
 LX_API lx_status lx_batch_get_march(const lx_batch* b, int* planar_rows, int* planes_3d);
 /* Picks the march per dimension by timing `steps` batched steps of each candidate on

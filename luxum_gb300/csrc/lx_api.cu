@@ -1710,8 +1710,17 @@ struct lx_batch {
   int chunk = 100;
   bool dirty = true;
   cudaStream_t stream = nullptr;
-  struct Group {  // members sharing (planar, uniform): one update launch per half step
+  // 3-D members of at least kSoloCells cells take one kernel pair each, with their parameter
+  // block passed by value (the constant bank, as for a handle stepped alone), spread over the
+  // batch stream and kLanes - 1 more so that the members' kernels overlap.
+  static constexpr long long kSoloCells = 1LL << 18;
+  static constexpr int kLanes = 4;
+  cudaStream_t lanes[kLanes - 1] = {};
+  cudaEvent_t lane_ev[kLanes] = {};  // [0] fork, [1..] joins
+  struct Group {  // members sharing (planar, uniform, solo): one update launch per half step
     bool planar = false, uniform = false;
+    bool solo = false;              // 3-D members launched one by one (kSoloCells and larger)
+    std::vector<char> host_params;  // solo groups: the members' parameter blocks
     int march = lx::kMarch3;   // cells each thread walks along x
     std::vector<int> members;  // batch-global indices
     void* d_params = nullptr;
@@ -1787,9 +1796,18 @@ extern "C" LX_API lx_status lx_batch_create(lx_batch** out) {
   if (!b) return fail(nullptr, LX_ERR_OOM, "host allocation failed");
   keep_pool_memory();
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  for (int l = 0; e == cudaSuccess && l < lx_batch::kLanes - 1; l++)
+    e = cudaStreamCreateWithFlags(&b->lanes[l], cudaStreamNonBlocking);
+  for (int l = 0; e == cudaSuccess && l < lx_batch::kLanes; l++)
+    e = cudaEventCreateWithFlags(&b->lane_ev[l], cudaEventDisableTiming);
   if (e != cudaSuccess) {
+    for (int l = 0; l < lx_batch::kLanes - 1; l++)
+      if (b->lanes[l]) cudaStreamDestroy(b->lanes[l]);
+    for (int l = 0; l < lx_batch::kLanes; l++)
+      if (b->lane_ev[l]) cudaEventDestroy(b->lane_ev[l]);
+    if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
-    return fail(nullptr, LX_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    return fail(nullptr, LX_ERR_CUDA, std::string("batch create: ") + cudaGetErrorString(e));
   }
   *out = b;
   return LX_OK;
@@ -1802,6 +1820,8 @@ extern "C" LX_API void lx_batch_destroy(lx_batch* b) {
   batch_free_device(b);
   cudaStreamSynchronize(b->stream);
   cudaStreamDestroy(b->stream);
+  for (int l = 0; l < lx_batch::kLanes - 1; l++) cudaStreamDestroy(b->lanes[l]);
+  for (int l = 0; l < lx_batch::kLanes; l++) cudaEventDestroy(b->lane_ev[l]);
   delete b;
 }
 
@@ -1892,13 +1912,17 @@ static lx_status batch_rebuild(lx_batch* b) {
       dft_planes[ci].push_back(dp);
       if (b->chunk > 0 && b->chunk % d.every != 0) b->graphable = false;
     }
+    const bool solo = !s->planar && (long long)s->Nx * s->Ny * s->Nz >= lx_batch::kSoloCells;
     int gi = -1;
     for (size_t g = 0; g < b->groups.size(); g++)
-      if (b->groups[g].planar == (bool)s->planar && b->groups[g].uniform == (bool)s->uniform) gi = (int)g;
+      if (b->groups[g].planar == (bool)s->planar && b->groups[g].uniform == (bool)s->uniform &&
+          b->groups[g].solo == solo)
+        gi = (int)g;
     if (gi < 0) {
       b->groups.emplace_back();
       b->groups.back().planar = s->planar;
       b->groups.back().uniform = s->uniform;
+      b->groups.back().solo = solo;
       b->groups.back().march = s->planar ? b->march2d : b->march3d;
       gi = (int)b->groups.size() - 1;
     }
@@ -1935,6 +1959,11 @@ static lx_status batch_rebuild(lx_batch* b) {
       if (nb > 0x7fffffffLL) return bfail(b, LX_ERR_INVALID, "batch too large for one launch");
       first.push_back((int)nb);
     }
+    if (g.solo) {  // launched by value from the host copy: no device blocks or tile map
+      g.host_params.assign((const char*)ps.data(), (const char*)(ps.data() + ps.size()));
+      g.nblocks = 0;
+      continue;
+    }
     g.nblocks = first.back();
     BCK(cudaMallocAsync(&g.d_params, sizeof(lx::StepParams<T, C>) * ps.size(), b->stream));
     BCK(cudaMemcpyAsync(g.d_params, ps.data(), sizeof(lx::StepParams<T, C>) * ps.size(), cudaMemcpyHostToDevice, b->stream));
@@ -1954,12 +1983,30 @@ static lx_status batch_enqueue(lx_batch* b, long long step0, int nsteps) {
   // the members' device step counters advance once, after the chunk; step q runs at ts + q
   for (int q = 0; q < nsteps; q++) {
     BCK(lx::launch_prologue_batch<C>(b->d_pps, b->d_ts, q, n, b->max_entries, b->stream));
-    for (auto& g : b->groups)
+    for (auto& g : b->groups) {
+      if (g.solo) {  // each member's H and E on one of the lanes; members are independent
+        const auto* hp = (const lx::StepParams<T, C>*)g.host_params.data();
+        const int L = std::min<int>(lx_batch::kLanes, (int)g.members.size());
+        BCK(cudaEventRecord(b->lane_ev[0], b->stream));
+        for (int l = 0; l < L - 1; l++) BCK(cudaStreamWaitEvent(b->lanes[l], b->lane_ev[0], 0));
+        for (size_t m = 0; m < g.members.size(); m++) {
+          cudaStream_t st = (m % L) ? b->lanes[m % L - 1] : b->stream;
+          BCK(lx::launch_step<T, C>(hp[m], false, g.uniform, true, st));
+          BCK(lx::launch_step<T, C>(hp[m], false, g.uniform, false, st));
+        }
+        for (int l = 0; l < L - 1; l++) {
+          BCK(cudaEventRecord(b->lane_ev[1 + l], b->lanes[l]));
+          BCK(cudaStreamWaitEvent(b->stream, b->lane_ev[1 + l], 0));
+        }
+        continue;
+      }
       BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.nblocks, g.planar,
                                       g.uniform, g.march, true, b->stream));
+    }
     for (auto& g : b->groups)
-      BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.nblocks, g.planar,
-                                      g.uniform, g.march, false, b->stream));
+      if (!g.solo)
+        BCK(lx::launch_batch_step<T, C>((const lx::StepParams<T, C>*)g.d_params, g.d_tiles, g.nblocks, g.planar,
+                                        g.uniform, g.march, false, b->stream));
     const long long bs = step0 + q;
     for (auto& cl : b->dft)
       if (bs % cl.every == cl.phase)
@@ -2080,6 +2127,7 @@ static lx_status tune_dimension(lx_batch* b, bool planar, int steps, double cell
   for (auto* s : b->sims) {
     if ((bool)s->planar != planar) continue;
     const double c = (double)s->Nx * s->Ny * s->Nz;
+    if (!planar && c >= (double)lx_batch::kSoloCells) continue;  // launched one by one: no tile shape
     if (!sample.empty() && cells + c > cell_budget) continue;
     sample.push_back(s);
     cells += c;

@@ -185,3 +185,46 @@ def test_member_changes_after_joining(engine):
     with pytest.raises(LuxumError):
         m.set_snapshots(5, 1 << 1, lambda *a: None)
     batch.close()
+
+
+def _cube(n, precision, pulse=False):
+    from luxum_gb300 import Sim
+
+    kw = dict(isPlanar=0, Nx=n + 2, Ny=n, Nz=n, precision=precision,
+              **cases.pw((1, 0, 0), (0, 0, 1), ((12, n - 11), (11, n - 12), (11, n - 12))), **cases.pml(8, kappa=15))
+    if pulse:
+        kw.update(usePS=1, source_kind=1, Nx_source=n // 2, Ny_source=n // 2, Nz_source=n // 3, amp_source=1.0,
+                  omega_source=2.0e11, src_t0=12.0, src_tw=5.0)
+    s = Sim(cases.make(**kw))
+    s.set_eps_box((n // 3, n // 3, n // 3), (n // 2, n // 2, n // 2), 5.0)
+    s.add_dft_plane(0, n // 2, 2 * np.pi * np.linspace(3e10, 1.5e11, 4), every=2)
+    return s
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_large_3d_members_launched_one_by_one(engine, precision):
+    """3-D members of 2^18 cells or more take one kernel pair each on four streams; with a
+    small 3-D member (the batched kernel) and a planar one, all equal their solo twins."""
+    from luxum_gb300 import Batch
+
+    def make():
+        return [_cube(64, precision), _cube(66, precision, pulse=True), _cube(70, precision), _cube(72, precision),
+                _cube(80, precision, pulse=True), _make("3d_pml_axis", precision), _make("planar_pml_axis", precision)]
+
+    members, twins = make(), make()
+    assert members[0].info()["cells"] >= 1 << 18 and members[5].info()["cells"] < 1 << 18
+    batch = Batch(chunk=10)
+    for m in members:
+        batch.add(m)
+    batch.step(25)  # graph replays and direct steps
+    for t in twins:
+        t.step(25)
+    for m, t in zip(members, twins):
+        _same(m, t)
+    members[1].step(3)  # a member steps alone between batch steps
+    twins[1].step(3)
+    batch.step(10)
+    for t in twins:
+        t.step(10)
+    for m, t in zip(members, twins):
+        _same(m, t)
