@@ -120,8 +120,9 @@ struct StepParams {
   // monitor / |E|^2 snapshot (E kernel)
   unsigned long long* max_slot;  // atomicMax of the bit pattern of max|E|^2 (non-negative)
   C* etotal;                     // when non-null, |E|^2 into the Ez-shaped array (3D)
-  // Single-sweep handles keep two copies of the state: after t steps it lives in buffer t & 1
-  // (buffer 0 = E, H, psiH, psiE above; buffer 1 here, null for handles updated in place).
+  // Second copy of the state, held by planar float-compute handles (null for the others; the
+  // in-place kernels ignore it).  For the single-sweep kernel, E, H, psiH, psiE name the copy
+  // it reads and E1, H1, psiH1, psiE1 the one it writes.
   T* E1[3];
   T* H1[3];
   C* psiH1[3][2];
