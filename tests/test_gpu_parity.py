@@ -174,14 +174,15 @@ def test_blowup_is_reported(engine):
     assert ei.value.status == 5
 
 
-@pytest.mark.parametrize("scale", ["mixed", "tiny", "huge", "sparse_denormal"])
+@pytest.mark.parametrize("scale", ["mixed", "tiny", "huge", "sparse_denormal", "near_equal", "planes"])
 def test_max_monitor_equals_etotal_max(engine, scale):
     """The max|E|^2 monitor (a block reduction on bit patterns, then atomicMax) equals, bit for
-    bit, the maximum of the |E|^2 array a twin keeps, for values from subnormal to huge."""
+    bit, the maximum of the |E|^2 array a twin keeps: values from subnormal to huge, near-equal
+    values and values constant over planes."""
     from luxum_gb300 import ETOTAL, Sim
 
     p, _, _ = cases.build("3d_pml_axis")
-    rng = np.random.default_rng({"mixed": 1, "tiny": 2, "huge": 3, "sparse_denormal": 4}[scale])
+    rng = np.random.default_rng({"mixed": 1, "tiny": 2, "huge": 3, "sparse_denormal": 4, "near_equal": 5, "planes": 6}[scale])
     a, b = Sim(p), Sim(p)
     for c in range(6):
         shp = a.shape(c)
@@ -191,6 +192,10 @@ def test_max_monitor_equals_etotal_max(engine, scale):
             v = rng.standard_normal(shp) * 1e-25
         elif scale == "huge":  # squares beyond float's range
             v = rng.standard_normal(shp) * 1e25
+        elif scale == "near_equal":  # every cell within 1e-9 of the others
+            v = 1.0 + rng.standard_normal(shp) * 1e-9
+        elif scale == "planes":  # one value per x plane, as in a plane wave
+            v = np.broadcast_to(rng.standard_normal((shp[0], 1, 1)), shp).copy()
         else:  # zeros with a few subnormal doubles
             v = np.zeros(shp)
             idx = tuple(rng.integers(0, n, 5) for n in shp)
