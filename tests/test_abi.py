@@ -149,3 +149,35 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert int(got[name]) == C.sizeof(py), name
         for field, _ in py._fields_:
             assert int(got[f"{name}.{field}"]) == getattr(py, field).offset, (name, field)
+
+
+@pytest.mark.parametrize("precision,two_buffers", [(0, False), (1, True), (2, True)])
+def test_device_bytes_counts_the_second_state_buffer(engine, monkeypatch, precision, two_buffers):
+    """Planar FP32 / FP16-storage handles keep two copies of E, H and psi (the single-sweep
+    step); lx_params_device_bytes, which the server admits requests by, counts both.  3-D and
+    FP64 handles keep one.  LUXUM_TWO_SWEEP=1 keeps new planar float handles at one copy."""
+    from luxum_gb300 import device_bytes, field_shape
+
+    kw = dict(isPlanar=1, Nx=300, Ny=1, Nz=520, precision=precision, **cases.pml(16))
+    p = cases.make(**kw)
+    monkeypatch.delenv("LUXUM_TWO_SWEEP", raising=False)
+    both = device_bytes(p)
+    monkeypatch.setenv("LUXUM_TWO_SWEEP", "1")
+    one = device_bytes(p)
+    if not two_buffers:
+        assert both == one
+        return
+    # the difference is one copy of Ey, Hx, Hz (padded rows) and of the four planar psi
+    # arrays (float): x slabs of Hz and Ey, n x Nzp each; z slabs of Hx and Ey, Nx x n each,
+    # with n the packed slab width (at most the 2 x 16 CPML cells)
+    tsize = {1: 4, 2: 2}[precision]
+    nzp = -(-520 * tsize // 128) * 128 // tsize
+    fields = 3 * 300 * nzp * tsize
+    per_cell_of_width = (2 * nzp + 2 * 300) * 4
+    psi = both - one - fields
+    assert psi % per_cell_of_width == 0 and 16 <= psi // per_cell_of_width <= 32
+    p3 = cases.make(isPlanar=0, Nx=40, Ny=40, Nz=40, precision=precision)
+    monkeypatch.delenv("LUXUM_TWO_SWEEP", raising=False)
+    a = device_bytes(p3)
+    monkeypatch.setenv("LUXUM_TWO_SWEEP", "1")
+    assert device_bytes(p3) == a
