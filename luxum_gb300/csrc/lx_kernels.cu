@@ -355,16 +355,60 @@ struct HMinBlocks {
   static constexpr int v = sizeof(C) == 4 ? 8 : 5;
 };
 
+// The z cells of a 3-D block.  Plain tiles are 32 consecutive cells.  With zends (FP64 grids
+// whose z CPML slabs are at most 16 cells wide), tile 0 is the row's two ends, k in [0, 16)
+// and [Nz-16, Nz), and tile m > 0 is [16 + 32(m-1), +32) up to Nz-16.  A plain row's first
+// and last tiles are half slab, and their warps run the z psi code with half the lanes idle;
+// the end tile runs it once with all lanes busy, and sixteen doubles keep the other tiles on
+// 128-byte lines.  Each lane has one cell (valid = inside its tile's range).
+struct ZTile {
+  int k;
+  bool valid;
+  int lo0, n0, lo1, n1;  // the tile's cells: [lo0, lo0+n0) and [lo1, lo1+n1)
+};
+
+__device__ __forceinline__ ZTile z_tile(int Nz, bool ends) {
+  ZTile z;
+  const int lane = threadIdx.x;
+  if (!ends) {
+    z.lo0 = blockIdx.x * 32;
+    z.n0 = 32;
+    z.lo1 = z.n1 = 0;
+    z.k = z.lo0 + lane;
+    z.valid = z.k < Nz;
+  } else if (blockIdx.x == 0) {
+    z.lo0 = 0;
+    z.n0 = 16;
+    z.lo1 = Nz - 16;
+    z.n1 = 16;
+    z.k = lane < 16 ? lane : Nz - 32 + lane;
+    z.valid = true;
+  } else {
+    z.lo0 = 16 + (blockIdx.x - 1) * 32;
+    z.n0 = min(32, Nz - 16 - z.lo0);
+    z.lo1 = z.n1 = 0;
+    z.k = z.lo0 + lane;
+    z.valid = lane < z.n0;
+  }
+  return z;
+}
+
+// Whether a 3-D block's tile meets a TF/SF plane, and whether it is interior.
+__device__ __forceinline__ bool ztile_meets_planes(const int (&pl)[3][2], int i, int j0, const ZTile& z) {
+  return tile_meets_planes(pl, i, 1, j0, 8, z.lo0, z.n0) || (z.n1 > 0 && tile_meets_planes(pl, i, 1, j0, 8, z.lo1, z.n1));
+}
+
 // One cell per thread; a block is 32 (z) x 8 (y) cells of one x plane.  Blocks whose tile is
 // interior take the cell code with every condition decided at compile time.
 template <class T, class C, bool UNI>
 __global__ void __launch_bounds__(256, HMinBlocks<C>::v) h_kernel_3d(const StepParams<T, C> p) {
-  const int k = blockIdx.x * 32 + threadIdx.x;
+  const ZTile z = z_tile(p.Nz, p.zends);
+  const int k = z.k;
   const int j = blockIdx.y * 8 + threadIdx.y;
   const int i = blockIdx.z;
-  if (k >= p.Nz || j >= p.Ny) return;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesH, i, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
-  if (!tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32))
+  if (!z.valid || j >= p.Ny) return;
+  const bool tf = p.tfsf && ztile_meets_planes(p.planesH, i, blockIdx.y * 8, z);
+  if (!tf && z.n1 == 0 && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * 8, 8, z.lo0, z.n0))
     h_cell_3d<T, C, UNI, true>(p, i, j, k, false);
   else
     h_cell_3d<T, C, UNI>(p, i, j, k, tf);
@@ -485,16 +529,17 @@ __device__ __forceinline__ typename MaxBits<C>::type e_cell_3d(const StepParams<
 
 template <class T, class C, bool UNI, bool MON>
 __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
-  const int k = blockIdx.x * 32 + threadIdx.x;
+  const ZTile z = z_tile(p.Nz, p.zends);
+  const int k = z.k;
   const int j = blockIdx.y * 8 + threadIdx.y;
   const int i = blockIdx.z;
-  const bool tf = p.tfsf && tile_meets_planes(p.planesE, i, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32);
+  const bool tf = p.tfsf && ztile_meets_planes(p.planesE, i, blockIdx.y * 8, z);
   typename MaxBits<C>::type mbits = 0;
   // The interior fast path pays for FP32 storage only (1.5 %); FP64 is bound by its pipe
   // either way, and FP16 storage ran 9 % slower with it.
   constexpr bool kFast = sizeof(T) == 4;
-  if (k < p.Nz && j < p.Ny) {
-    if (kFast && !tf && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * 8, 8, blockIdx.x * 32, 32))
+  if (z.valid && j < p.Ny) {
+    if (kFast && !tf && z.n1 == 0 && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * 8, 8, z.lo0, z.n0))
       mbits = e_cell_3d<T, C, UNI, MON, kFast>(p, i, j, k, false);
     else
       mbits = e_cell_3d<T, C, UNI, MON>(p, i, j, k, tf);
@@ -1230,16 +1275,20 @@ cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bo
       else e_kernel_2d<T, C, false, false><<<grid, block, 0, s>>>(p);
     }
   } else {
-    dim3 grid((p.Nz + 31) / 32, (p.Ny + 7) / 8, p.Nx);
+    // FP64 with z CPML slabs of at most 16 cells: the rows' two ends share one tile (ZTile)
+    StepParams<T, C> q = p;
+    q.zends = sizeof(T) == 8 && p.pml && p.slab[2].n > 0 && p.slab[2].lo <= 16 && p.Nz - p.slab[2].hi0 <= 16 &&
+              p.Nz >= 48;
+    dim3 grid(q.zends ? 1 + (p.Nz - 32 + 31) / 32 : (p.Nz + 31) / 32, (p.Ny + 7) / 8, p.Nx);
     if (h_half) {
-      if (uniform) h_kernel_3d<T, C, true><<<grid, block, 0, s>>>(p);
-      else h_kernel_3d<T, C, false><<<grid, block, 0, s>>>(p);
+      if (uniform) h_kernel_3d<T, C, true><<<grid, block, 0, s>>>(q);
+      else h_kernel_3d<T, C, false><<<grid, block, 0, s>>>(q);
     } else if (mon) {
-      if (uniform) e_kernel_3d<T, C, true, true><<<grid, block, 0, s>>>(p);
-      else e_kernel_3d<T, C, false, true><<<grid, block, 0, s>>>(p);
+      if (uniform) e_kernel_3d<T, C, true, true><<<grid, block, 0, s>>>(q);
+      else e_kernel_3d<T, C, false, true><<<grid, block, 0, s>>>(q);
     } else {
-      if (uniform) e_kernel_3d<T, C, true, false><<<grid, block, 0, s>>>(p);
-      else e_kernel_3d<T, C, false, false><<<grid, block, 0, s>>>(p);
+      if (uniform) e_kernel_3d<T, C, true, false><<<grid, block, 0, s>>>(q);
+      else e_kernel_3d<T, C, false, false><<<grid, block, 0, s>>>(q);
     }
   }
   return cudaGetLastError();
