@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
-"""Headline benchmark of the GB300 FDTD engine.
+"""Benchmarks of the GB300 FDTD engine.
 
-Workload (one bench step = one whole simulation): 3-D Yee grid 256^3, FP64, 1000 time
+Headline (one bench step = one whole simulation): 3-D Yee grid 256^3, FP64, 1000 time
 steps; x-directed Gaussian plane wave (pulse 1/e half-width 14.1 cells = 28 steps) injected
 through a TF/SF box [32,223]^3 that sits 16 cells inside a 16-cell CPML (m=3, kappa 15);
 centred 48^3 dielectric cube eps_r = 6; snapshots of Ex..Hz every 250 steps; 8 seeded
@@ -13,9 +13,17 @@ value : Gcell-updates/s with the material already resident on the GPU (fields re
 e2e   : the same through the public API from host buffers: each step uploads the three
         material arrays from pinned memory and reads back every snapshot and the probe
         series.
-roofline: the dominant kernel's algorithmic bytes per launch / its mean CUDA-event time.
+roofline: FP64 bound.  The dominant update kernel's FP64 pipe instructions per launch over
+        its mean CUDA-event time, against the FP64 FMA issue rate of a measured cuBLAS
+        DGEMM; beside it the HBM fraction of the whole step (compulsory bytes per step from
+        lx_params_step_bytes over ms_per_step) and of the dominant kernel alone.
+configs: the other configurations, each with its own HBM roofline (compulsory bytes per
+        cell update x cell updates / wall time): the 512^2 planar CPML run (FP64), the
+        photonic-crystal precision study (FP64/FP32/FP16 storage, errors vs FP64), the
+        256-lens batch (FP32) and a shortened Poisson serving stream (p50/p99).
 cpu_baseline / --impl reference: the oracle (CPU restatement of the reference's loops,
-        OpenMP like the reference) on the host cores, on a bounded sample of the workload.
+        OpenMP like the reference, built -O3 like it) on the host cores, one process x all
+        threads, on bounded samples of each configuration, with and without snapshot writes.
 """
 from __future__ import annotations
 
@@ -185,27 +193,57 @@ def fp64_peak_tflops(torch) -> float:
 
 
 def kernel_model(sim, p):
-    """Algorithmic bytes and FP64 flops per launch of the H and E kernels.
+    """Algorithmic bytes and FP64 pipe instructions per launch of the H and E kernels.
 
     Bytes: every array a kernel must touch, once: H kernel reads E (3) and H (3) and writes
     H (3); E kernel reads H (3), E (3), Cb (3) and writes E (3); each stored psi entry is
-    read and written once.  Flops per component: 3 differences + 1 FMA (5 flops); per psi
-    term: psi = b*psi + c*d and d/kappa + psi (5 flops); with the max monitor every step the
-    E kernel also forms |E|^2 = Ex^2 + Ey^2 + Ez^2 per cell (5 flops, no extra bytes).
+    read and written once.  FP64 instructions per component: 2 differences, 1 subtraction
+    and 1 FMA (4); per psi term: psi = b*psi + c*d (a multiply and an FMA) and d/kappa + psi
+    (an FMA), 3; with the max monitor every step the E kernel also forms
+    |E|^2 = Ex^2 + Ey^2 + Ez^2 per cell (a multiply and two FMAs, 3).  Flops count an FMA as 2.
     """
     info = sim.info()
     el = info["field_bytes"]
     cel = 8 if p.precision == 0 else 4
     cells = info["cells"]
     psi_h, psi_e = info["psi_h_entries"], info["psi_e_entries"]
+    mon = p.monitor_every == 1
     h_bytes = cells * 9 * el + psi_h * 2 * cel
     e_bytes = cells * 9 * el + cells * 3 * cel + psi_e * 2 * cel
+    h_ops = cells * 12 + psi_h * 3
+    e_ops = cells * 12 + psi_e * 3 + (cells * 3 if mon else 0)
     h_flops = cells * 15 + psi_h * 5
-    e_flops = cells * 15 + psi_e * 5 + (cells * 5 if p.monitor_every == 1 else 0)
-    return {"h_update": (h_bytes, h_flops), "e_update": (e_bytes, e_flops)}
+    e_flops = cells * 15 + psi_e * 5 + (cells * 5 if mon else 0)
+    return {"h_update": (h_bytes, h_ops, h_flops), "e_update": (e_bytes, e_ops, e_flops)}
 
 
-def run_cpu_sample(steps: int, threads: int):
+def hbm_roof(bytes_per_step: float, steps: float, seconds: float, peak: float, peak_kind: str, **extra):
+    """HBM roofline of a run: compulsory bytes per time step x time steps / wall time."""
+    achieved = bytes_per_step * steps / seconds / 1e9
+    d = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+         "peak_source": peak_kind, "bytes_per_step": bytes_per_step}
+    d.update(extra)
+    return d
+
+
+# ------------------------------------------------------------------ CPU baseline (the oracle port)
+
+def cpu_info(threads: int) -> dict:
+    """One process (the reference's MPI is absent here, so one rank) x `threads` OpenMP threads."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"ranks": 1, "threads": threads, "cores": threads, "cpu_model": model, "host_cpus": os.cpu_count(),
+            "build": "gcc -O3 -fopenmp -ffp-contract=off (the reference builds with -O3, src/solvers/CMakeLists.txt:22)"}
+
+
+def _dropin_oracle(threads: int):
     from oracle.oracle import OracleSim
 
     p = workload_params(0)
@@ -213,6 +251,12 @@ def run_cpu_sample(steps: int, threads: int):
     for c in range(3):
         o.set_material(c, material(o.shape(c)), 1e6)
     o.step(1)  # first touch of the arrays
+    return o
+
+
+def run_cpu_sample(steps: int, threads: int):
+    """`steps` time steps of the 256^3 workload on the oracle; (Gcell-updates/s, seconds)."""
+    o = _dropin_oracle(threads)
     t0 = time.perf_counter()
     o.step(steps)
     dt = time.perf_counter() - t0
@@ -220,19 +264,122 @@ def run_cpu_sample(steps: int, threads: int):
     return N ** 3 * steps / dt / 1e9, dt
 
 
-def lens_sims(n_sims: int, seed: int, precision: int, steps: int):
-    """The batch workload: planar lens simulations of uneven size (seeded).
+def _write_cost(o, comps, tmpdir: str) -> float:
+    """Seconds to write one snapshot of `comps` (their contiguous doubles, one file each)."""
+    t0 = time.perf_counter()
+    for c in comps:
+        o.append_raw(c, os.path.join(tmpdir, f"snap{c}.raw"))
+    dt = time.perf_counter() - t0
+    for c in comps:
+        os.remove(os.path.join(tmpdir, f"snap{c}.raw"))
+    return dt
+
+
+def cpu_dropin(steps: int, threads: int) -> dict:
+    """The 256^3 drop-in on the oracle: `steps` time steps timed without writes, one Ex..Hz
+    snapshot write timed on its own, the 1000-step run (4 snapshots) extrapolated from both."""
+    import tempfile
+
+    o = _dropin_oracle(threads)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    with tempfile.TemporaryDirectory() as d:
+        snap = _write_cost(o, range(6), d)
+    o.close()
+    run_s = dt * STEPS / steps
+    return {"value": N ** 3 * steps / dt / 1e9, "unit": UNIT,
+            "value_with_snapshots": N ** 3 * STEPS / (run_s + 4 * snap) / 1e9,
+            "sample": f"{steps} time steps of the 1000-step 256^3 run ({N ** 3 * steps:.3g} cell-updates, {dt:.1f} s); "
+                      f"one Ex..Hz snapshot write ({6 * 8 * N ** 3 / 1e9:.2f} GB, {snap:.2f} s) timed separately; "
+                      "value_with_snapshots extrapolates to 1000 steps with 4 snapshots"}
+
+
+def cpu_planar_full(threads: int) -> dict:
+    """The 512^2 planar CPML configuration on the oracle, all 2000 steps, without and with the
+    driver's Ey writes every 10 steps (two_dim_pml.cc:184)."""
+    import tempfile
+
+    from oracle.oracle import OracleSim
+
+    out = {}
+    for writes in (False, True):
+        o = OracleSim(planar_params(0, 512), threads=threads)
+        o.set_eps_box((224, 0, 224), (288, 1, 288), 10.89)
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "Ey.raw")
+            t0 = time.perf_counter()
+            if writes:
+                for t in range(2000):
+                    o.step(1)
+                    if t % 10 == 0:
+                        o.append_raw(1, path)
+            else:
+                o.step(2000)
+            dt = time.perf_counter() - t0
+        o.close()
+        out["value_with_snapshots" if writes else "value"] = 512 * 512 * 2000 / dt / 1e9
+        out["seconds_with_snapshots" if writes else "seconds"] = dt
+    out.update(unit=UNIT, sample="the full 2000-step run, without and with the 200 Ey writes")
+    return out
+
+
+def cpu_phc_window(steps: int, threads: int) -> dict:
+    """A window of the photonic-crystal run on the oracle (FP64, both DFT planes), extrapolated."""
+    from oracle.oracle import OracleSim
+
+    c = PHC
+    g_params = phc_params(0)
+    o = OracleSim(g_params, threads=threads)
+    for lo, hi, eps in phc_rods():
+        o.set_eps_box(lo, hi, eps)
+    o.add_dft_plane(0, 40, PHC_OMEGA, every=5)
+    o.add_dft_plane(0, 470, PHC_OMEGA, every=5)
+    o.step(1)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    cells = c["nx"] * c["ny"] * c["nz"]
+    v = cells * steps / dt / 1e9
+    return {"value": v, "unit": UNIT, "sample": f"{steps}-step window of the 4000-step run ({dt:.1f} s); the full "
+                                                f"run extrapolates to {cells * c['steps'] / v / 1e9 / 60:.0f} min"}
+
+
+def cpu_lens_subset(n_sims: int, steps: int, threads: int) -> dict:
+    """The first `n_sims` lens simulations of the batch workload, `steps` steps each, one after
+    the other on the oracle (the reference runs one simulation per invocation)."""
+    from oracle.oracle import OracleSim
+
+    work = 0
+    dt = 0.0
+    for p, F in lens_specs(n_sims, 4, 0, steps):
+        o = OracleSim(p, threads=threads)
+        o.set_material(1, F, 1.0)
+        o.step(1)
+        t0 = time.perf_counter()
+        o.step(steps)
+        dt += time.perf_counter() - t0
+        work += p.Nx * p.Nz * steps
+        o.close()
+    v = work / dt / 1e9
+    return {"value": v, "unit": UNIT, "sample": f"{n_sims} of the 256 simulations, {steps} of their 3000 steps each "
+                                                f"({work:.3g} cell-updates, {dt:.1f} s)"}
+
+
+def lens_specs(n_sims: int, seed: int, precision: int, steps: int):
+    """The batch workload: planar lens simulations of uneven size (seeded), as (params, F).
 
     Side N ~ U{128..1024}; half elliptic lenses (semi-axes 10-40 % of N, eps_r ~ U(1.5, 2.25)),
     half distorted lenses (same ellipse with a sinusoidal boundary perturbation of up to
     5 cells); Ey plane wave at normal incidence from the left through a TF/SF box 16 cells
     inside a 16-cell CPML (textbook CPML sign, kappa 5, a_max 0.05).  The lens enters as the
-    material array F of Cb = dt/(eps0*(1+F)), i.e. F = eps_r - 1.
+    material array F of Cb = dt/(eps0*(1+F)), i.e. F = eps_r - 1 on Ey (scale 1).
     """
-    from luxum_gb300 import Sim, params
+    from luxum_gb300 import params
 
     rng = np.random.default_rng(seed)
-    sims = []
+    out = []
     for q in range(n_sims):
         n = int(rng.integers(128, 1025))
         box = (32, n - 33)
@@ -240,7 +387,6 @@ def lens_sims(n_sims: int, seed: int, precision: int, steps: int):
                    kx_pw=1.0, Ey_pw=1.0, off_pw=24.0, x1_pw=box[0], x2_pw=box[1], z1_pw=box[0], z2_pw=box[1],
                    usePML=1, d_pml=0.016, sigma=0.65, sigma_m=3.0, kappa=5.0, a_max=0.05, a_m=1.0,
                    cpml_mode=1, precision=precision)
-        s = Sim(p)
         a, b = rng.uniform(0.1, 0.4, 2) * n
         eps = rng.uniform(1.5, 2.25)
         x = np.arange(n)[:, None] - n / 2
@@ -253,7 +399,17 @@ def lens_sims(n_sims: int, seed: int, precision: int, steps: int):
             inside = np.sqrt(r2) <= 1.0 + amp * np.sin(m * th + rng.uniform(0, 2 * np.pi))
         else:
             inside = r2 <= 1.0
-        F = np.where(inside, eps - 1.0, 0.0).reshape(n, 1, n)
+        out.append((p, np.where(inside, eps - 1.0, 0.0).reshape(n, 1, n)))
+    return out
+
+
+def lens_sims(n_sims: int, seed: int, precision: int, steps: int):
+    """Handles of lens_specs' simulations, with their lens maps on the device."""
+    from luxum_gb300 import Sim
+
+    sims = []
+    for p, F in lens_specs(n_sims, seed, precision, steps):
+        s = Sim(p)
         s.set_material(1, F, 1.0)
         sims.append(s)
     return sims
@@ -284,19 +440,16 @@ def box_sims(n_sims: int, seed: int, precision: int, steps: int):
     return sims
 
 
-def bench_batch(args):
-    """--config batch: 256 uneven planar simulations stepped as one batch (batch3d: 3-D cubes)."""
+def run_batch(n_sims: int, steps: int, three: bool, runs: int, solo_sample: int, solo_steps: int, peak: float,
+              peak_kind: str) -> dict:
+    """Uneven simulations stepped as one batch: planar lenses, or 3-D cubes (three)."""
     import torch
 
-    import __graft_entry__
+    from luxum_gb300 import Batch, step_bytes
 
-    __graft_entry__.build()
-    from luxum_gb300 import Batch
-
-    steps = args.batch_steps
-    three = args.config == "batch3d"
-    sims = box_sims(args.batch_sims, 6, 1, steps) if three else lens_sims(args.batch_sims, 4, 1, steps)
+    sims = box_sims(n_sims, 6, 1, steps) if three else lens_sims(n_sims, 4, 1, steps)
     cells = sum(s.p.Nx * s.p.Ny * s.p.Nz for s in sims)
+    bytes_step = sum(step_bytes(s.p) for s in sims)
     batch = Batch(chunk=100)
     for s in sims:
         batch.add(s)
@@ -313,13 +466,13 @@ def bench_batch(args):
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(runs):
             run()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-    value = cells * steps * args.steps / dt / 1e9
+    value = cells * steps * runs / dt / 1e9
     # the same simulations one by one (unbatched), on a sample
-    sample = sims[: args.solo_sample]
+    sample = sims[:solo_sample]
     scells = sum(s.p.Nx * s.p.Ny * s.p.Nz for s in sample)
     for s in sample:
         s.reset()
@@ -328,24 +481,36 @@ def bench_batch(args):
     t0 = time.perf_counter()
     for s in sample:
         s.reset()
-        s.step(args.solo_steps)
+        s.step(solo_steps)
         s.sync()
-    solo = scells * args.solo_steps / (time.perf_counter() - t0) / 1e9
+    solo = scells * solo_steps / (time.perf_counter() - t0) / 1e9
     desc = (f"batch of {len(sims)} 3-D simulations, cubes of side U{{64..192}} seed 6, CPML min(16, side/8), TF/SF "
             f"plane wave, 1-4 eps boxes, FP32, {steps} steps, graph chunks of 100" if three else
             f"batch of {len(sims)} planar lens simulations, sides U{{128..1024}} seed 4, "
             f"CPML 16, TF/SF normal incidence, FP32, {steps} steps, graph chunks of 100")
-    line = {"config": {"workload": desc,
-                       "cells": cells, "cell_updates_per_run": cells * steps},
-            "metric": "Gcell-updates/s (batched)", "value": value, "unit": UNIT, "runs": args.steps,
-            "s_per_run": dt / args.steps, "dtype": "f32",
-            "unbatched_sample": {"sims": len(sample), "value": solo, "steps": args.solo_steps,
+    batch.close()
+    for s in sims:
+        s.close()
+    return {"config": {"workload": desc, "cells": cells, "cell_updates_per_run": cells * steps,
+                       "l2": f"no flush: resident state {bytes_step / 2 ** 30:.1f} GiB of traffic per step >> 129 MB L2"},
+            "metric": "Gcell-updates/s (batched)", "value": value, "unit": UNIT, "runs": runs,
+            "s_per_run": dt / runs, "dtype": "f32",
+            "roofline": hbm_roof(bytes_step, steps * runs, dt, peak, peak_kind, bytes_per_cell_update=bytes_step / cells),
+            "unbatched_sample": {"sims": len(sample), "value": solo, "steps": solo_steps,
                                  "note": "same simulations stepped one handle at a time with lx_sim_step"},
             "batched_over_unbatched": value / solo, "autotuned_march": {"planar_rows": march[0], "planes_3d": march[1],
                                                                        "seconds": t_tune},
             "clocks": clk.summary()}
-    print(json.dumps(line), flush=True)
-    batch.close()
+
+
+def bench_batch(args):
+    """--config batch: 256 uneven planar simulations stepped as one batch (batch3d: 3-D cubes)."""
+    import __graft_entry__
+
+    __graft_entry__.build()
+    peak, kind = measured_peaks()
+    print(json.dumps(run_batch(args.batch_sims, args.batch_steps, args.config == "batch3d", args.steps,
+                               args.solo_sample, args.solo_steps, peak, kind)), flush=True)
 
 
 def serve_requests(n: int, seed: int, rate: float):
@@ -396,18 +561,15 @@ def serve_params(req):
     return params(isPlanar=0, Nx=n, Ny=n, Nz=n, Ez_pw=1.0, **kw)
 
 
-def bench_serve(args):
-    """--config serve: a Poisson request stream through the native server (lx_server_*):
-    continuous batching under an HBM budget, latency taken by the server's own clock."""
+def run_serve(n_requests: int, rate: float, budget_gb: float, chunk: int, peak: float, peak_kind: str) -> dict:
+    """A Poisson request stream through the native server (lx_server_*): continuous batching
+    under an HBM budget, latency taken by the server's own clock."""
     import torch
 
-    import __graft_entry__
+    from luxum_gb300 import LX_PREC_FP32, Server, step_bytes
 
-    __graft_entry__.build()
-    from luxum_gb300 import LX_PREC_FP32, Server
-
-    reqs = serve_requests(args.serve_requests, 5, args.serve_rate)
-    srv = Server(precision=LX_PREC_FP32, chunk=args.serve_chunk, budget_bytes=args.serve_budget_gb * 1e9)
+    reqs = serve_requests(n_requests, 5, rate)
+    srv = Server(precision=LX_PREC_FP32, chunk=chunk, budget_bytes=budget_gb * 1e9)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ids = []
@@ -418,7 +580,7 @@ def bench_serve(args):
                 time.sleep(d)
             plane = r["side"] - 1 - 2 * serve_margin(r["side"]) - 4
             ids.append(srv.submit(serve_params(r), SERVE_STEPS, r["boxes"], (0, plane, SERVE_OMEGA, 10)))
-        lat, work, failed = [], 0, 0
+        lat, work, failed, traffic = [], 0, 0, 0.0
         for rid, r in zip(ids, reqs):
             if srv.wait(rid) != "done":
                 failed += 1
@@ -428,61 +590,88 @@ def bench_serve(args):
             t = srv.times(rid)
             lat.append(t[2] - t[0])
             work += r["side"] ** (2 if r["planar"] else 3) * SERVE_STEPS
+            traffic += step_bytes(serve_params(r)) * SERVE_STEPS
             srv.release(rid)
         wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
     lat = np.array(lat)
     offered = sum(r["side"] ** (2 if r["planar"] else 3) for r in reqs) * SERVE_STEPS / reqs[-1]["arrival"] / 1e9
-    line = {"config": {"workload": f"{len(reqs)} requests, Poisson {args.serve_rate}/s (seed 5), 80% planar 256-2048, "
+    return {"config": {"workload": f"{len(reqs)} requests, Poisson {rate}/s (seed 5), 80% planar 256-2048, "
                                    f"20% 3-D 64-256, 1-8 eps boxes, {SERVE_STEPS} steps FP32, FP64 DFT 64 freqs at one "
-                                   f"plane (sampled every 10 steps), budget {args.serve_budget_gb} GB, chunk "
-                                   f"{args.serve_chunk}; native server (lx_server_*)"},
+                                   f"plane (sampled every 10 steps), budget {budget_gb} GB, chunk {chunk}; native "
+                                   "server (lx_server_*)"},
             "metric": "p50/p99 latency and aggregate Gcell-updates/s", "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "value": work / wall / 1e9,
             "unit": UNIT, "offered_gcells": offered, "wall_s": wall, "completed": int(lat.size), "failed": failed,
+            "roofline": hbm_roof(traffic, 1, wall, peak, peak_kind, bytes_per_cell_update=traffic / max(work, 1),
+                                 note="compulsory bytes of every completed request over the stream's wall time"),
+            "sustained": bool(work / wall / 1e9 >= 0.95 * offered),
             "peak_running": st["peak_running"], "peak_budget_gb": st["peak_bytes_running"] / 1e9,
             "chunks": st["chunks"], "gpu_busy_s": st["busy_seconds"], "dtype": "f32", "clocks": clk.summary()}
-    print(json.dumps(line), flush=True)
+
+
+def bench_serve(args):
+    """--config serve: the full request stream (1000 requests by default)."""
+    import __graft_entry__
+
+    __graft_entry__.build()
+    peak, kind = measured_peaks()
+    print(json.dumps(run_serve(args.serve_requests, args.serve_rate, args.serve_budget_gb, args.serve_chunk, peak,
+                               kind)), flush=True)
 
 
 PHC = dict(nx=512, ny=512, nz=128, steps=4000, cpml=20, period=40, rod=16, eps=12.0)
 PHC_OMEGA = 2 * np.pi * np.linspace(2.0e9, 3.6e9, 64)
 
 
-def phc_sim(precision: int):
-    """Photonic-crystal waveguide: square eps_r 12 rods (16x16 cells, period 40, full height) with
-    the row nearest mid-y removed; CPML 20; Gaussian-pulsed sine on Ez at the defect entrance
-    (omega 1.76e10 rad/s = 2.8 GHz, width 159 steps, centred at step 480); FP64 DFT planes
-    (64 frequencies, 2.0-3.6 GHz) across the guide at x = 40 (input) and x = 470 (output)."""
-    from luxum_gb300 import Sim, params
+def phc_params(precision: int):
+    """Photonic-crystal waveguide: CPML 20; Gaussian-pulsed sine on Ez at the defect entrance
+    (omega 1.76e10 rad/s = 2.8 GHz, width 159 steps, centred at step 480)."""
+    from luxum_gb300 import params
 
     c = PHC
     p = params(isPlanar=0, Nx=c["nx"], Ny=c["ny"], Nz=c["nz"], dx=1e-3, dy=1e-3, dz=1e-3, S=0.5,
                num_timesteps=c["steps"], usePML=1, d_pml=c["cpml"] * 1e-3, sigma=0.65, sigma_m=3.0, kappa=5.0,
                a_max=0.05, a_m=1.0, cpml_mode=1, usePS=1, source_kind=1, amp_source=1.0,
                omega_source=2 * np.pi * 2.8e9, src_t0=480.0, src_tw=159.0, precision=precision)
+    p.Nx_source, p.Ny_source, p.Nz_source = c["cpml"] + 4, phc_defect(), c["nz"] // 2
+    return p
+
+
+def phc_defect() -> int:
+    centres = [20 + PHC["period"] * m for m in range(13)]
+    return min(centres, key=lambda y: abs(y - PHC["ny"] // 2))
+
+
+def phc_rods():
+    """Square eps_r 12 rods (16x16 cells, period 40, full height), the row nearest mid-y
+    removed: (lo, hi, eps_r) boxes."""
+    c = PHC
     centres = [20 + c["period"] * m for m in range(13)]
-    defect = min(centres, key=lambda y: abs(y - c["ny"] // 2))
-    p.Nx_source, p.Ny_source, p.Nz_source = c["cpml"] + 4, defect, c["nz"] // 2
-    s = Sim(p)
     h = c["rod"] // 2
-    for xc in centres:
-        for yc in centres:
-            if yc == defect:
-                continue
-            s.set_eps_box((xc - h, yc - h, 0), (xc + h, yc + h, c["nz"]), c["eps"])
+    return [((xc - h, yc - h, 0), (xc + h, yc + h, c["nz"]), c["eps"])
+            for xc in centres for yc in centres if yc != phc_defect()]
+
+
+def phc_sim(precision: int):
+    """The waveguide with FP64 DFT planes (64 frequencies, 2.0-3.6 GHz) across the guide at
+    x = 40 (input) and x = 470 (output)."""
+    from luxum_gb300 import Sim
+
+    s = Sim(phc_params(precision))
+    for lo, hi, eps in phc_rods():
+        s.set_eps_box(lo, hi, eps)
     planes = (s.add_dft_plane(0, 40, PHC_OMEGA, every=5), s.add_dft_plane(0, 470, PHC_OMEGA, every=5))
     return s, planes
 
 
-def bench_phc(args):
-    """--config phc: the waveguide run in FP64, FP32 and FP16 storage; errors against FP64."""
+def run_phc(peak: float, peak_kind: str) -> dict:
+    """The waveguide run in FP64, FP32 and FP16 storage; errors against FP64."""
     import torch
 
-    import __graft_entry__
+    from luxum_gb300 import step_bytes
 
-    __graft_entry__.build()
     c = PHC
     cells = c["nx"] * c["ny"] * c["nz"]
     out = {}
@@ -499,7 +688,9 @@ def bench_phc(args):
         fin, fout = s.dft_flux(pin), s.dft_flux(pout)
         T = fout / np.where(np.abs(fin) > 0, fin, np.nan)
         fields = [s.field(k) for k in range(6)]
-        entry = {"value": cells * c["steps"] / dt / 1e9, "unit": UNIT, "seconds": dt}
+        sb = step_bytes(s.p)
+        entry = {"value": cells * c["steps"] / dt / 1e9, "unit": UNIT, "seconds": dt,
+                 "roofline": hbm_roof(sb, c["steps"], dt, peak, peak_kind, bytes_per_cell_update=sb / cells)}
         if ref is None:
             ref = (fields, T, fin, fout)
             entry["transmission"] = {"f_ghz": (PHC_OMEGA[::8] / 2 / np.pi / 1e9).round(3).tolist(),
@@ -523,11 +714,61 @@ def bench_phc(args):
         out[name] = entry
         del fields
         s.close()
-    line = {"config": {"workload": "3-D photonic-crystal waveguide 512x512x128, eps_r 12 rods 16x16 cells period 40 "
+    return {"config": {"workload": "3-D photonic-crystal waveguide 512x512x128, eps_r 12 rods 16x16 cells period 40 "
                                    "with a one-row line defect, CPML 20, pulsed Ez point source, 4000 steps; FP64 DFT "
-                                   "transmission (64 frequencies 2.0-3.6 GHz, planes x=40 and x=470)"},
+                                   "transmission (64 frequencies 2.0-3.6 GHz, planes x=40 and x=470)",
+                       "l2": "no flush: resident state >= 1.5 GB >> 129 MB L2"},
             "metric": "Gcell-updates/s and error vs FP64 per precision", "results": out}
-    print(json.dumps(line), flush=True)
+
+
+def bench_phc(args):
+    """--config phc: the waveguide run in FP64, FP32 and FP16 storage; errors against FP64."""
+    import __graft_entry__
+
+    __graft_entry__.build()
+    peak, kind = measured_peaks()
+    print(json.dumps(run_phc(peak, kind)), flush=True)
+
+
+def run_planar(runs: int, peak: float, peak_kind: str) -> dict:
+    """The 512^2 planar CPML configuration (FP64, 2000 steps, Ey snapshots every 10 steps as
+    two_dim_pml.cc:184 writes them, max|E|^2 every step), `runs` runs after one untimed."""
+    import torch
+
+    from luxum_gb300 import Sim, step_bytes
+
+    p = planar_params(0, 512)
+    p.num_timesteps = 2000
+    s = Sim(p)
+    s.set_eps_box((224, 0, 224), (288, 1, 288), 10.89)
+    stream = torch.cuda.current_stream()
+    s.set_stream(stream.cuda_stream)
+    s.set_snapshots(10, 1 << 1, lambda t, comp, arr: None)
+
+    def one():
+        s.reset()
+        s.step(2000)
+        s.sync()
+
+    one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(runs):
+        one()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) * 1e-3
+    kt = s.time_kernels(200)
+    sb = step_bytes(p)
+    s.close()
+    return {"config": {"workload": "2-D 512x512 (x-z plane, Ey), FP64, 2000 steps, TF/SF box [30,481]^2 normal "
+                                   "incidence, eps_r 10.89 square [224,288)^2, CPML 20 (m=3, kappa 5, a_max 0.05), "
+                                   "Ey snapshot every 10 steps staged to pinned host memory, max|E|^2 every step",
+                       "l2": "state 9 MB: L2-resident, so the HBM fraction is not a bound here"},
+            "value": 512 * 512 * 2000 * runs / sec / 1e9, "unit": UNIT, "runs": runs, "s_per_run": sec / runs,
+            "dtype": "f64", "kernel_ms": kt,
+            "roofline": hbm_roof(sb, 2000 * runs, sec, peak, peak_kind, bytes_per_cell_update=sb / 512 ** 2)}
 
 
 def dist_setup(n_gpus: int, backend: str | None = None):
@@ -580,16 +821,18 @@ def bench_reference(args):
         vals.append(v)
         t_all += dt
     value = float(np.mean(vals))
+    cpu = cpu_info(threads)
+    cpu.update(value=value, unit=UNIT, kind="port",
+               sample=f"{sample} time steps of the 256^3 workload per bench step ({N ** 3 * sample:.3g} "
+                      "cell-updates), no snapshot writes; the reference needs blitz++, yaml-cpp 0.3, MPI and HDF5 "
+                      "and is not buildable here, so its loops run as the oracle restatement (same loop nests, "
+                      "OpenMP, FP64)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_dict(f"each step: {sample} time steps of the 1000-step run"),
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{sample} time steps of the 256^3 workload per bench step "
-                                       f"({N ** 3 * sample:.3g} cell-updates); the reference needs blitz++, "
-                                       "yaml-cpp 0.3, MPI and HDF5 and is not buildable here, so its loops run "
-                                       "as the oracle restatement (same loop nests, OpenMP, FP64)"}}
+            "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
 
 
@@ -610,9 +853,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample-steps", type=int, default=20)
+    ap.add_argument("--cpu-sample-steps", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the FP32 / FP16-storage lines")
+    ap.add_argument("--no-suite", action="store_true", help="skip the other configurations (planar, phc, batch, serve)")
+    ap.add_argument("--suite-serve-requests", type=int, default=200, help="requests of the serving stream in the suite")
+    ap.add_argument("--cpu-phc-steps", type=int, default=20)
+    ap.add_argument("--cpu-lens-steps", type=int, default=200)
     ap.add_argument("--profile", type=int, default=0, metavar="N",
                     help="run the N^3 profiling case instead of the benchmark (for ncu)")
     ap.add_argument("--profile-steps", type=int, default=4)
@@ -654,7 +901,7 @@ def main():
         __graft_entry__.build()
     if pg:
         pg.barrier()
-    from luxum_gb300 import Sim
+    from luxum_gb300 import Sim, step_bytes
 
     p = workload_params(0)
     sim = Sim(p)
@@ -730,22 +977,30 @@ def main():
     e2e = {"value": job_rate(N ** 3 * STEPS * args.steps, world, ms_e2e), "unit": UNIT,
            "h2d_bytes_per_step": (h2d1 - h2d0) // args.steps, "d2h_bytes_per_step": (d2h1 - d2h0) // args.steps}
 
-    # ---- per-kernel roofline (instrumented pass, events around each launch)
+    # ---- roofline: FP64 pipe of the dominant update kernel (instrumented pass, events around
+    # each launch), then the HBM fractions of the whole step and of that kernel
     sim.reset()
     sim.step(120)  # wave inside the box, psi active
     kt = sim.time_kernels(40)
     model = kernel_model(sim, p)
     dom = max(("h_update", "e_update"), key=lambda k: kt[k])
-    bytes_alg, flops_alg = model[dom]
+    bytes_alg, ops_alg, flops_alg = model[dom]
     peak_bw, peak_kind = measured_peaks()
-    achieved = bytes_alg / (kt[dom] * 1e-3) / 1e9
-    fp64_peak = fp64_peak_tflops(torch)
-    fp64_ach = flops_alg / (kt[dom] * 1e-3) / 1e12
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_bw, "unit": "GB/s", "frac": achieved / peak_bw,
-                "traffic": None, "kernel": dom, "peak_source": peak_kind,
-                "bytes_per_launch": bytes_alg, "ms_per_launch": kt[dom],
-                "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
-                         "flops_per_launch": flops_alg, "peak_source": "measured cuBLAS DGEMM 8192^3"},
+    fp64_peak = fp64_peak_tflops(torch)  # FLOP/s of a DGEMM: FMA instructions at half this rate
+    ops_rate = ops_alg / (kt[dom] * 1e-3) / 1e12
+    step_b = step_bytes(p)
+    roofline = {"bound": "fp64", "achieved": ops_rate, "peak": fp64_peak / 2, "unit": "T FP64 instructions/s",
+                "frac": ops_rate / (fp64_peak / 2), "traffic": None, "kernel": dom,
+                "peak_source": "measured cuBLAS DGEMM 8192^3 (FP64 FMA issue rate = its FLOP/s / 2)",
+                "ops_per_launch": ops_alg, "ms_per_launch": kt[dom],
+                "flops": {"achieved_tflops": flops_alg / (kt[dom] * 1e-3) / 1e12, "peak_tflops": fp64_peak,
+                          "frac": flops_alg / (kt[dom] * 1e-3) / 1e12 / fp64_peak, "flops_per_launch": flops_alg},
+                "hbm_step": hbm_roof(step_b, STEPS * args.steps, ms * 1e-3, peak_bw, peak_kind,
+                                     bytes_per_cell_update=step_b / N ** 3,
+                                     note="compulsory bytes per step (lx_params_step_bytes) over ms_per_step"),
+                "hbm_kernel": {"achieved": bytes_alg / (kt[dom] * 1e-3) / 1e9, "peak": peak_bw, "unit": "GB/s",
+                               "frac": bytes_alg / (kt[dom] * 1e-3) / 1e9 / peak_bw, "bytes_per_launch": bytes_alg,
+                               "note": "the dominant kernel's own compulsory bytes over its launch time"},
                 "kernel_ms": kt}
     traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic_file):
@@ -754,6 +1009,7 @@ def main():
                 tr = json.load(f).get(dom)
             if tr:
                 roofline["traffic"] = tr["bytes_per_launch"]
+                roofline["traffic_unit"] = "bytes per launch (DRAM read + write)"
                 roofline["traffic_source"] = tr["source"]
         except (OSError, ValueError):
             pass
@@ -791,9 +1047,12 @@ def main():
                 den = sum(float(np.linalg.norm(ref[c])) ** 2 for c in comps)
                 errs[grp] = (num / den) ** 0.5 if den else None
             kq = q.time_kernels(40)
+            qb = step_bytes(q.p)
             precision[name] = {"value": cell_updates / (qms * 1e-3) / 1e9, "unit": UNIT,
                                "ms_per_step": qms / args.steps, "speedup_vs_fp64": ms / qms,
-                               "rel_l2_vs_fp64_after_1000_steps": errs, "kernel_ms": kq}
+                               "rel_l2_vs_fp64_after_1000_steps": errs, "kernel_ms": kq,
+                               "roofline": hbm_roof(qb, STEPS * args.steps, qms * 1e-3, peak_bw, peak_kind,
+                                                    bytes_per_cell_update=qb / N ** 3)}
             q.close()
         del ref
 
@@ -803,13 +1062,24 @@ def main():
             "e2e": e2e, "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches,
             "max_e2_final": sim.max_e2(), "precision_forms": precision}
     sim.close()
+    if rank == 0 and world == 1 and not args.no_suite:
+        line["configs"] = {
+            "planar_512_fp64": run_planar(5, peak_bw, peak_kind),
+            "phc_precision_study": run_phc(peak_bw, peak_kind),
+            "lens_batch_fp32": run_batch(256, 3000, False, 1, args.solo_sample, args.solo_steps, peak_bw, peak_kind),
+            "serving_stream": run_serve(args.suite_serve_requests, args.serve_rate, args.serve_budget_gb,
+                                        args.serve_chunk, peak_bw, peak_kind)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, dt = run_cpu_sample(args.cpu_sample_steps, threads)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{args.cpu_sample_steps} time steps of this workload "
-                                          f"({N ** 3 * args.cpu_sample_steps:.3g} cell-updates, {dt:.1f} s) run by "
-                                          "the oracle restatement of the reference's OpenMP loops"}
+        cpu = cpu_info(threads)
+        drop = cpu_dropin(args.cpu_sample_steps, threads)
+        cpu.update(value=drop["value"], unit=UNIT, kind="port", sample=drop["sample"],
+                   value_with_snapshots=drop["value_with_snapshots"])
+        if not args.no_suite:
+            cpu["configs"] = {"planar_512_fp64": cpu_planar_full(threads),
+                              "phc_precision_study": cpu_phc_window(args.cpu_phc_steps, threads),
+                              "lens_batch_fp32": cpu_lens_subset(16, args.cpu_lens_steps, threads)}
+        line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg:

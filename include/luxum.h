@@ -138,6 +138,12 @@ LX_API void lx_sim_destroy(lx_sim* sim);
  * DFT planes and transfer buffers come on top when used.  Serving loops admit requests
  * against an HBM budget with it. */
 LX_API lx_status lx_params_device_bytes(const lx_params* p, size_t* bytes);
+/* Compulsory device-memory traffic of one time step for *p, computed on the host: every
+ * field component read and written once, every Cb array read once and every stored CPML psi
+ * entry read and written once, over the Nx*Ny*Nz cells (padding excluded), at the storage
+ * sizes of p->precision.  The figure a roofline divides by the step time.  Measurement aid
+ * with no counterpart in the reference (whose drivers move about four times as much). */
+LX_API lx_status lx_params_step_bytes(const lx_params* p, double* bytes);
 /* Zeroes E, H, psi and |E|^2 and rewinds to step 0 (the state after lx_sim_create); keeps
  * Cb, probe positions and snapshot outputs, so one handle can run many simulations. */
 LX_API lx_status lx_sim_reset(lx_sim* sim);

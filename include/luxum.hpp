@@ -76,9 +76,11 @@ class maxwell {
     }
     const auto t0 = std::chrono::steady_clock::now();
     // Steps run in chunks; the max of each step comes back from the device series once per
-    // chunk.  The drivers print, at the top of step t, the max left by step t-1
-    // (two_dim_pml.cc:135-141); at t = 0 they print an uninitialised local_max, here 0 (the
-    // max of the zero initial fields).
+    // chunk.  solve_planar prints, after its E update, the max of step t itself
+    // (two_dim.cc:126-137).  The other three drivers print, at the top of step t, the max left
+    // by step t-1 (two_dim_pml.cc:135-141, three_dim.cc:91-97, three_dim_pml.cc:167-173); at
+    // t = 0 they print an uninitialised local_max, here 0 (the max of the zero initial fields).
+    const bool same_step = planar && !pml;
     const int chunk = 100;
     check(lx_sim_set_max_series(sim_, chunk), sim_);
     std::vector<int> ts(chunk);
@@ -91,7 +93,8 @@ class maxwell {
       int rows = 0;
       check(lx_sim_read_max_series(sim_, ts.data(), ms.data(), chunk, &rows), sim_);
       for (int r = 0; r < rows; r++) {
-        if (!quiet && print_every > 0 && ts[r] % print_every == 0) std::printf("t: %d, max: %g\n", ts[r], prev);
+        const double shown = same_step ? ms[r] : prev;
+        if (!quiet && print_every > 0 && ts[r] % print_every == 0) std::printf("t: %d, max: %g\n", ts[r], shown);
         prev = ms[r];
       }
       done += n;

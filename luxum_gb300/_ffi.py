@@ -99,6 +99,7 @@ def declare(lib) -> None:
     _proto(lib, "lx_sim_create", C.c_int, P(Params), P(C.c_void_p))
     _proto(lib, "lx_sim_destroy", None, sim)
     _proto(lib, "lx_params_device_bytes", C.c_int, P(Params), P(C.c_size_t))
+    _proto(lib, "lx_params_step_bytes", C.c_int, P(Params), P(C.c_double))
     _proto(lib, "lx_sim_reset", C.c_int, sim)
     _proto(lib, "lx_sim_set_cb", C.c_int, sim, C.c_int, P(C.c_double), C.c_size_t)
     _proto(lib, "lx_sim_set_material", C.c_int, sim, C.c_int, P(C.c_double), C.c_size_t, C.c_double)

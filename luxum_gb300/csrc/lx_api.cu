@@ -374,6 +374,7 @@ static lx_status settle(lx_sim* s) {
 
 extern "C" LX_API void lx_sim_destroy(lx_sim* s) {
   if (!s) return;
+  lx::DeviceGuard dg_(s->device);
   if (s->batch) lx_batch_remove(s->batch, s);
   stop_writer(s);
   if (s->stream) cudaStreamSynchronize(s->stream);
@@ -657,8 +658,36 @@ extern "C" LX_API lx_status lx_params_device_bytes(const lx_params* p, size_t* b
   return LX_OK;
 }
 
+extern "C" LX_API lx_status lx_params_step_bytes(const lx_params* p, double* bytes) {
+  if (!p || !bytes) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  std::string why;
+  lx_status st = validate(p, why);
+  if (st) return fail(nullptr, st, why);
+  lx_sim tmp;
+  setup_host(&tmp, p);
+  const double cells = (double)p->Nx * (tmp.planar ? 1 : p->Ny) * p->Nz;
+  const int nF = tmp.planar ? 3 : 6, nE = tmp.planar ? 1 : 3;
+  double b = cells * (2.0 * nF * tmp.tsize + (double)nE * tmp.csize);
+  if (tmp.pml) {
+    const double ext[3] = {(double)p->Nx, tmp.planar ? 1.0 : (double)p->Ny, (double)p->Nz};
+    for (int a = 0; a < 3; a++) {
+      if (tmp.planar && a == 1) continue;
+      const int N = a == 0 ? p->Nx : (a == 1 ? p->Ny : p->Nz);
+      const double delta = a == 0 ? p->dx : (a == 1 ? p->dy : p->dz);
+      AxisProf ap;
+      axis_profiles(tmp.k, p->cpml_mode, N, delta, ap);
+      const Slab sl = make_slab(ap, N);
+      // psi arrays whose derivative runs along axis a: 2 H + 2 E in 3-D, 1 + 1 in planar
+      b += 2.0 * (tmp.planar ? 2 : 4) * sl.n * (cells / ext[a]) * tmp.csize;
+    }
+  }
+  *bytes = b;
+  return LX_OK;
+}
+
 extern "C" LX_API lx_status lx_sim_reset(lx_sim* s) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   lx_status st = lx_sim_sync(s);
   if (st) return st;
   const size_t fb = s->ncell * s->tsize;
@@ -696,13 +725,15 @@ static lx_status ensure_xfer(lx_sim* s) {
 // The buffer holding the current state (buffer t & 1 in ping-pong mode, else 0), and the other.
 static bool odd_state(const lx_sim* s) { return s->pp && (s->t & 1); }
 
-static void* comp_ptr(lx_sim* s, int comp, bool other = false) {
+void* lx::comp_ptr(lx_sim* s, int comp, bool other) {
   const bool b1 = odd_state(s) != other;
   if (comp >= LX_EX && comp <= LX_EZ) return b1 ? s->E1[comp] : s->E[comp];
   if (comp >= LX_HX && comp <= LX_HZ) return b1 ? s->H1[comp - 3] : s->H[comp - 3];
   if (comp == LX_ETOTAL) return other ? nullptr : s->etotal;
   return nullptr;
 }
+
+using lx::comp_ptr;
 
 static void* psi_ptr(lx_sim* s, bool h, int a, int q, bool other = false) {
   const bool b1 = odd_state(s) != other;
@@ -762,6 +793,7 @@ extern "C" LX_API lx_status lx_sim_field_shape(const lx_sim* s, int comp, int sh
 
 extern "C" LX_API lx_status lx_sim_read_field(lx_sim* s, int comp, double* host, size_t n) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   if (comp < 0 || comp > LX_ETOTAL) return fail(s, LX_ERR_INVALID, "bad component");
   const size_t m = ext_n(s, comp);
@@ -800,6 +832,7 @@ static lx_status upload(lx_sim* s, const double* host, size_t m) {
 
 extern "C" LX_API lx_status lx_sim_write_field(lx_sim* s, int comp, const double* host, size_t n) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   if (comp < 0 || comp > LX_HZ) return fail(s, LX_ERR_INVALID, "bad component");
   const size_t m = ext_n(s, comp);
@@ -871,6 +904,7 @@ lx_status raw_to_device(lx_sim* s, void* dev, const std::vector<double>& in) {
 
 extern "C" LX_API lx_status lx_sim_save(lx_sim* s, const char* path) {
   if (!s || !path) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   lx_status st = lx_sim_sync(s);
   if (st) return st;
   if ((st = ensure_xfer(s))) return st;
@@ -933,6 +967,7 @@ extern "C" LX_API lx_status lx_sim_save(lx_sim* s, const char* path) {
 
 extern "C" LX_API lx_status lx_sim_load(lx_sim* s, const char* path) {
   if (!s || !path) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   lx_status st = lx_sim_sync(s);
   if (st) return st;
   std::vector<double> v;
@@ -994,6 +1029,7 @@ static lx_status check_cb_comp(lx_sim* s, int comp, size_t n) {
 
 extern "C" LX_API lx_status lx_sim_set_cb(lx_sim* s, int comp, const double* cb, size_t n) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   lx_status st = check_cb_comp(s, comp, n);
   if (st) return st;
@@ -1005,6 +1041,7 @@ extern "C" LX_API lx_status lx_sim_set_cb(lx_sim* s, int comp, const double* cb,
 
 extern "C" LX_API lx_status lx_sim_set_material(lx_sim* s, int comp, const double* F, size_t n, double scale) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   lx_status st = check_cb_comp(s, comp, n);
   if (st) return st;
@@ -1016,6 +1053,7 @@ extern "C" LX_API lx_status lx_sim_set_material(lx_sim* s, int comp, const doubl
 
 extern "C" LX_API lx_status lx_sim_set_eps_box(lx_sim* s, const int lo[3], const int hi[3], double eps_r) {
   if (!s || !lo || !hi) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   if (!(eps_r > 0)) return fail(s, LX_ERR_INVALID, "eps_r must be > 0");
   const double val = s->k.dt / (s->k.epsilon0 * eps_r) * s->cbs_scale;
@@ -1033,6 +1071,7 @@ extern "C" LX_API lx_status lx_sim_set_eps_box(lx_sim* s, const int lo[3], const
 
 extern "C" LX_API lx_status lx_sim_set_probes(lx_sim* s, const int* ijk, int nprobes, int cap) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   if (s->batch)
     return fail(s, LX_ERR_STATE, "remove the handle from its batch first: batched members keep no snapshot outputs or probes");
   if (nprobes < 0 || nprobes > lx::kMaxProbes || cap < 0) return fail(s, LX_ERR_INVALID, "0..64 probes, capacity >= 0");
@@ -1057,6 +1096,7 @@ extern "C" LX_API lx_status lx_sim_set_probes(lx_sim* s, const int* ijk, int npr
 
 extern "C" LX_API lx_status lx_sim_read_probes(lx_sim* s, double* host, size_t n, int* rows) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   const size_t m = (size_t)s->probe_rows * s->nprobes * 6;
   if (rows) *rows = s->probe_rows;
@@ -1073,6 +1113,7 @@ extern "C" LX_API lx_status lx_sim_read_probes(lx_sim* s, double* host, size_t n
 extern "C" LX_API lx_status lx_sim_add_dft_plane(lx_sim* s, int axis, int index, int nfreq, const double* omega,
                                                  int every, int* id) {
   if (!s || !omega || !id) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   if (axis < 0 || axis > 2 || (s->planar && axis == 1)) return fail(s, LX_ERR_INVALID, "axis must be 0, 1 or 2 (planar: 0 or 2)");
   const int N[3] = {s->Nx, s->Ny, s->Nz};
@@ -1105,6 +1146,7 @@ extern "C" LX_API lx_status lx_sim_add_dft_plane(lx_sim* s, int axis, int index,
 
 extern "C" LX_API lx_status lx_sim_read_dft(lx_sim* s, int id, double* host, size_t n) {
   if (!s || !host) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   if (id < 0 || id >= (int)s->dfts.size()) return fail(s, LX_ERR_INVALID, "no such DFT plane");
   const lx::DftPlane& d = s->dfts[id];
@@ -1117,6 +1159,7 @@ extern "C" LX_API lx_status lx_sim_read_dft(lx_sim* s, int id, double* host, siz
 
 extern "C" LX_API lx_status lx_sim_dft_flux(lx_sim* s, int id, double* flux, int nfreq) {
   if (!s || !flux) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   if (id < 0 || id >= (int)s->dfts.size()) return fail(s, LX_ERR_INVALID, "no such DFT plane");
   lx::DftPlane& d = s->dfts[id];
@@ -1229,6 +1272,7 @@ static lx_status add_output(lx_sim* s, const lx::Output& o) {
 
 extern "C" LX_API lx_status lx_sim_set_snapshots(lx_sim* s, int every, unsigned mask, lx_snapshot_fn fn, void* user) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   if (s->batch)
     return fail(s, LX_ERR_STATE, "remove the handle from its batch first: batched members keep no snapshot outputs or probes");
   if (every < 0 || (every > 0 && !fn)) return fail(s, LX_ERR_INVALID, "every >= 0 and a callback are required");
@@ -1251,6 +1295,7 @@ extern "C" LX_API lx_status lx_sim_set_snapshots(lx_sim* s, int every, unsigned 
 
 extern "C" LX_API lx_status lx_sim_set_hdf5_output(lx_sim* s, int every, int first, int comp, const char* path) {
   if (!s || !path) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   if (s->batch)
     return fail(s, LX_ERR_STATE, "remove the handle from its batch first: batched members keep no snapshot outputs or probes");
   if (every <= 0 || first < 0 || comp < 0 || comp > LX_ETOTAL || ext_n(s, comp) == 0)
@@ -1313,6 +1358,7 @@ static lx_status snapshot(lx_sim* s, int t, unsigned mask) {
 
 extern "C" LX_API lx_status lx_sim_sync(lx_sim* s) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaStreamSynchronize(s->side));
@@ -1570,6 +1616,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
 
 extern "C" LX_API lx_status lx_sim_step(lx_sim* s, int nsteps) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   if (nsteps < 0) return fail(s, LX_ERR_INVALID, "nsteps must be >= 0");
   {
@@ -1587,6 +1634,7 @@ extern "C" LX_API lx_status lx_sim_step(lx_sim* s, int nsteps) {
 
 extern "C" LX_API lx_status lx_sim_time_kernels(lx_sim* s, int nsteps, double out_ms[4]) {
   if (!s || !out_ms) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   if (nsteps < 1) return fail(s, LX_ERR_INVALID, "nsteps must be >= 1");
   KernelTimer kt;
@@ -1606,6 +1654,7 @@ extern "C" LX_API int lx_sim_timestep(const lx_sim* s) { return s ? s->t : -1; }
 
 extern "C" LX_API lx_status lx_sim_set_max_series(lx_sim* s, int capacity) {
   if (!s || capacity < 0) return fail(s, LX_ERR_INVALID, "capacity must be >= 0");
+  lx::DeviceGuard dg_(s->device);
   if (s->batch) return fail(s, LX_ERR_STATE, "batched members keep no max series");
   lx_status st = lx_sim_sync(s);
   if (st) return st;
@@ -1623,6 +1672,7 @@ extern "C" LX_API lx_status lx_sim_set_max_series(lx_sim* s, int capacity) {
 
 extern "C" LX_API lx_status lx_sim_read_max_series(lx_sim* s, int* steps, double* values, int capacity, int* rows) {
   if (!s || !rows) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   lx_status st = lx_sim_sync(s);
   if (st) return st;
   const int n = (int)s->series_t.size();
@@ -1643,6 +1693,7 @@ extern "C" LX_API lx_status lx_sim_read_max_series(lx_sim* s, int* steps, double
 
 extern "C" LX_API lx_status lx_sim_max_e2(lx_sim* s, double* out) {
   if (!s || !out) return fail(s, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(s->device);
   { const lx_status st_ = settle(s); if (st_) return st_; }
   *out = s->last_max;
   return LX_OK;
@@ -1650,6 +1701,7 @@ extern "C" LX_API lx_status lx_sim_max_e2(lx_sim* s, double* out) {
 
 extern "C" LX_API lx_status lx_sim_set_stream(lx_sim* s, void* stream) {
   if (!s) return fail(nullptr, LX_ERR_INVALID, "null handle");
+  lx::DeviceGuard dg_(s->device);
   lx_status st = lx_sim_sync(s);
   if (st) return st;
   s->stream = stream ? (cudaStream_t)stream : s->own;
@@ -1706,6 +1758,7 @@ extern "C" LX_API void lx_host_free(void* ptr) {
 
 struct lx_batch {
   std::vector<lx_sim*> sims;
+  int device = 0;  // CUDA device current at lx_batch_create; every member lives on it
   int prec = -1;
   int chunk = 100;
   bool dirty = true;
@@ -1795,6 +1848,7 @@ extern "C" LX_API lx_status lx_batch_create(lx_batch** out) {
   lx_batch* b = new (std::nothrow) lx_batch();
   if (!b) return fail(nullptr, LX_ERR_OOM, "host allocation failed");
   keep_pool_memory();
+  cudaGetDevice(&b->device);
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   for (int l = 0; e == cudaSuccess && l < lx_batch::kLanes - 1; l++)
     e = cudaStreamCreateWithFlags(&b->lanes[l], cudaStreamNonBlocking);
@@ -1815,6 +1869,7 @@ extern "C" LX_API lx_status lx_batch_create(lx_batch** out) {
 
 extern "C" LX_API void lx_batch_destroy(lx_batch* b) {
   if (!b) return;
+  lx::DeviceGuard dg_(b->device);
   cudaStreamSynchronize(b->stream);
   for (auto* s : b->sims) s->batch = nullptr;
   batch_free_device(b);
@@ -1829,6 +1884,7 @@ extern "C" LX_API int lx_batch_size(const lx_batch* b) { return b ? (int)b->sims
 
 extern "C" LX_API lx_status lx_batch_set_chunk(lx_batch* b, int steps) {
   if (!b || steps < 0) return fail(nullptr, LX_ERR_INVALID, "chunk must be >= 0");
+  lx::DeviceGuard dg_(b->device);
   b->chunk = steps;
   if (b->exec) cudaGraphExecDestroy(b->exec);
   b->exec = nullptr;
@@ -1840,9 +1896,11 @@ extern "C" LX_API lx_status lx_batch_wait(lx_batch* b);
 
 extern "C" LX_API lx_status lx_batch_add(lx_batch* b, lx_sim* s) {
   if (!b || !s) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(b->device);
   lx_status st = lx_batch_wait(b);
   if (st) return st;
   if (s->batch) return bfail(b, LX_ERR_INVALID, s->batch == b ? "handle already in this batch" : "handle is in another batch");
+  if (s->device != b->device) return bfail(b, LX_ERR_INVALID, "the handle lives on another device than the batch");
   if (b->prec >= 0 && s->prec != b->prec) return bfail(b, LX_ERR_INVALID, "all members of a batch share one precision");
   if (!s->outputs.empty() || s->nprobes > 0 || s->d_series)
     return bfail(b, LX_ERR_UNSUPPORTED, "batched members cannot have snapshot outputs, probes or a max series");
@@ -1857,6 +1915,7 @@ extern "C" LX_API lx_status lx_batch_add(lx_batch* b, lx_sim* s) {
 
 extern "C" LX_API lx_status lx_batch_remove(lx_batch* b, lx_sim* s) {
   if (!b || !s) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(b->device);
   lx_status st = lx_batch_wait(b);
   if (st) return st;
   for (size_t q = 0; q < b->sims.size(); q++)
@@ -2064,6 +2123,7 @@ static lx_status batch_run_async(lx_batch* b, int nsteps) {
 
 extern "C" LX_API lx_status lx_batch_step_async(lx_batch* b, int nsteps) {
   if (!b || nsteps < 0) return fail(nullptr, LX_ERR_INVALID, "bad argument");
+  lx::DeviceGuard dg_(b->device);
   if (b->sims.empty() || nsteps == 0) return LX_OK;
   if (b->prec == LX_PREC_FP64) return batch_run_async<double, double>(b, nsteps);
   if (b->prec == LX_PREC_FP32) return batch_run_async<float, float>(b, nsteps);
@@ -2072,6 +2132,7 @@ extern "C" LX_API lx_status lx_batch_step_async(lx_batch* b, int nsteps) {
 
 extern "C" LX_API lx_status lx_batch_wait(lx_batch* b) {
   if (!b) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  lx::DeviceGuard dg_(b->device);
   if (b->pending == 0) return LX_OK;
   const int n = (int)b->sims.size();
   std::vector<unsigned long long> slots(n);
@@ -2099,6 +2160,7 @@ static bool march_ok(int m) { return m == 1 || m == 2 || m == 4 || m == 8; }
 
 extern "C" LX_API lx_status lx_batch_set_march(lx_batch* b, int planar_rows, int planes_3d) {
   if (!b || !march_ok(planar_rows) || !march_ok(planes_3d)) return fail(nullptr, LX_ERR_INVALID, "march must be 1, 2, 4 or 8");
+  lx::DeviceGuard dg_(b->device);
   lx_status st = lx_batch_wait(b);
   if (st) return st;
   b->march2d = planar_rows;
@@ -2179,6 +2241,7 @@ static lx_status tune_dimension(lx_batch* b, bool planar, int steps, double cell
 
 extern "C" LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* planar_rows, int* planes_3d) {
   if (!b || steps < 1) return fail(nullptr, LX_ERR_INVALID, "steps must be >= 1");
+  lx::DeviceGuard dg_(b->device);
   lx_status st = lx_batch_wait(b);
   if (st) return st;
   int m2 = 0, m3 = 0;

@@ -18,6 +18,7 @@
 #include "lx_hdf5.h"
 
 #include <algorithm>
+#include <cerrno>
 #include <cstdint>
 #include <cstring>
 #include <sstream>
@@ -80,12 +81,17 @@ std::string dataset_name(int t) {
 
 Hdf5Writer::~Hdf5Writer() { close(); }
 
+std::string Hdf5Writer::failed(const char* what) const {
+  return std::string(what) + " failed on " + path_ + ": " + std::strerror(errno);
+}
+
 std::string Hdf5Writer::open(const char* path, const int ext[3]) {
   f_ = std::fopen(path, "wb+");
-  if (!f_) return std::string("cannot create ") + path;
+  if (!f_) return std::string("cannot create ") + path + ": " + std::strerror(errno);
+  path_ = path;
   for (int a = 0; a < 3; a++) ext_[a] = ext[a];
   std::vector<uint8_t> zeros(96, 0);
-  if (std::fwrite(zeros.data(), 1, zeros.size(), f_) != zeros.size()) return "write failed";
+  if (std::fwrite(zeros.data(), 1, zeros.size(), f_) != zeros.size()) return failed("write");
   eof_ = 96;
   return "";
 }
@@ -101,9 +107,9 @@ std::string Hdf5Writer::write_named(const std::string& name, const double* data,
   for (int a = 0; a < 3; a++) e.ext[a] = ext[a];
   e.addr = eof_;
   e.bytes = n * 8;
-  if (std::fseek(f_, (long)eof_, SEEK_SET) != 0) return "seek failed";
+  if (std::fseek(f_, (long)eof_, SEEK_SET) != 0) return failed("seek");
   // native double is little-endian IEEE on every host this builds for
-  if (n && std::fwrite(data, 8, n, f_) != n) return "write failed";
+  if (n && std::fwrite(data, 8, n, f_) != n) return failed("write");
   eof_ += e.bytes;
   while (eof_ % 8) {
     std::fputc(0, f_);
@@ -230,10 +236,10 @@ std::string Hdf5Writer::close() {
   put64(sb, heap_addr);
   std::string err;
   if (std::fseek(f_, (long)base, SEEK_SET) != 0 || std::fwrite(meta.data(), 1, meta.size(), f_) != meta.size())
-    err = "metadata write failed";
+    err = failed("metadata write");
   if (err.empty() && (std::fseek(f_, 0, SEEK_SET) != 0 || std::fwrite(sb.data(), 1, sb.size(), f_) != sb.size()))
-    err = "superblock write failed";
-  if (std::fclose(f_) != 0 && err.empty()) err = "close failed";
+    err = failed("superblock write");
+  if (std::fclose(f_) != 0 && err.empty()) err = failed("close");
   f_ = nullptr;
   return err;
 }

@@ -23,7 +23,9 @@ class Hdf5Writer {
     unsigned long long addr, bytes;
     int ext[3];
   };
+  std::string failed(const char* what) const;  // "<what> failed on <path>: <errno text>"
   std::FILE* f_ = nullptr;
+  std::string path_;
   int ext_[3] = {0, 0, 0};
   unsigned long long eof_ = 0;
   std::vector<Entry> entries_;

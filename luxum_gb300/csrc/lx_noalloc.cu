@@ -13,8 +13,9 @@
 // (8 MiB).  Every GPU that loads the library holds it until the process exits, whether or
 // not the entry point is ever called.  Its host-side name is only a stand-in for the symbol:
 // the device address is looked up once per device with cudaGetSymbolAddress, on the first
-// call made while that device is current, and cached.  Because that first call performs
-// the lookup, it should be made before any stream capture begins.
+// call for a handle of that device (with that device made current for the call), and cached.
+// Because that first call performs the lookup, it should be made before any stream capture
+// begins.
 //
 // Every call on a device shares the one array and leaves the last call's data in it.  Calls
 // whose device work overlaps (two handles read on different streams at once, or two host
@@ -43,12 +44,11 @@ __device__ __align__(256) double g_noalloc_staging[kLxNoAllocMaxElems];
 std::mutex g_mu;
 double* g_staging_ptr[kMaxDevices] = {};
 
-// Device address of the staging array on the current device (looked up once per device).
-cudaError_t staging_address(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
+// Device address of the staging array on device `dev`, which the caller has made current
+// (looked up once per device).
+cudaError_t staging_address(int dev, double** out) {
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  cudaError_t e;
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_staging_ptr[dev]) {
     void* p = nullptr;
@@ -90,6 +90,7 @@ void launch(const void* src, double* dst, const int ext[3], int Ny, int Nzp, dou
 
 extern "C" LX_API lx_status lx_sim_read_field_noalloc(lx_sim* s, int comp, double* host, size_t n) {
   if (!s || !host) return lx::set_thread_error("null argument", LX_ERR_INVALID);
+  lx::DeviceGuard dg_(s->device);  // the handle's device, for the lookup and the launch
   auto bad = [&](lx_status st, const std::string& m) {
     s->err = m;
     return lx::set_thread_error(m.c_str(), st);
@@ -105,12 +106,10 @@ extern "C" LX_API lx_status lx_sim_read_field_noalloc(lx_sim* s, int comp, doubl
     const lx_status st = lx_batch_wait(s->batch);
     if (st && st != LX_ERR_BLOWUP) return st;
   }
-  const bool b1 = s->pp && (s->t & 1);  // ping-pong mode: the state after t steps is in buffer t & 1
-  const void* src = comp <= LX_EZ ? (b1 ? s->E1[comp] : s->E[comp])
-                                  : (comp <= LX_HZ ? (b1 ? s->H1[comp - 3] : s->H[comp - 3]) : s->etotal);
+  const void* src = lx::comp_ptr(s, comp);  // the buffer holding the state after t steps
   if (!src) return bad(LX_ERR_STATE, comp == LX_ETOTAL ? "|E|^2 is only kept when a snapshot asks for it" : "component absent");
   double* staging = nullptr;
-  cudaError_t e = staging_address(&staging);
+  cudaError_t e = staging_address(s->device, &staging);
   if (e != cudaSuccess) return bad(LX_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
   const bool compute_prec = comp == LX_ETOTAL;
   const double mul = (comp >= LX_HX && comp <= LX_HZ) ? 1.0 / s->hscale : 1.0;

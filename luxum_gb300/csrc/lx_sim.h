@@ -52,6 +52,25 @@ struct SnapJob {
   size_t off[7];
 };
 
+// Makes a handle's device current for the length of an entry point and gives the caller's
+// device back on return.  A handle's streams and memory belong to the device that was current
+// when it was created; a caller on another device would otherwise launch on the wrong one.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != device && cudaSetDevice(device) == cudaSuccess) prev_ = cur;
+  }
+  ~DeviceGuard() {
+    if (prev_ >= 0) cudaSetDevice(prev_);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+ private:
+  int prev_ = -1;
+};
+
 // Host-side constants of maxwell::maxwell (maxwell.cc:60-148).
 struct Consts {
   double epsilon0, mew0, S, c, dt, dx, dy, dz, sigma, init;
@@ -134,3 +153,11 @@ struct lx_sim {
   // counters
   uint64_t n_kernels = 0, n_h2d = 0, n_d2h = 0;
 };
+
+namespace lx {
+// Device array of component `comp` (LX_EX..LX_ETOTAL) in the buffer that holds the current
+// state: buffer t & 1 for a handle stepped alone in ping-pong mode, else buffer 0.  With
+// `other`, the buffer that does not.  Null when the handle keeps no such array.  Every reader
+// of a handle's fields takes its source from here.
+void* comp_ptr(lx_sim* s, int comp, bool other = false);
+}  // namespace lx

@@ -37,6 +37,16 @@ def device_bytes(p: Params) -> int:
     return n.value
 
 
+def step_bytes(p: Params) -> float:
+    """Compulsory device-memory bytes of one time step for p (host-only): every field read
+    and written once, Cb read once, every stored CPML psi entry read and written once."""
+    b = C.c_double()
+    st = _ffi.lib().lx_params_step_bytes(C.byref(p), C.byref(b))
+    if st:
+        raise LuxumError(st, _ffi.lib().lx_last_error(None).decode())
+    return b.value
+
+
 def field_shape(p: Params, comp: int) -> tuple:
     """Staggered extent of a component for parameters p (host only)."""
     shp = (C.c_int * 3)()

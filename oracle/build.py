@@ -1,8 +1,9 @@
 """Build recipe of the oracle (test infrastructure): liboracle.so from luxum_oracle.c.
 
-gcc -O2 -fopenmp -ffp-contract=off: OpenMP mirrors the reference's `omp parallel for`
-loops (used when the CPU baseline is timed); no FMA contraction, so results are the same
-on x86-64 and aarch64 hosts.
+gcc -O3 -fopenmp -ffp-contract=off: -O3 as the reference's own build (src/solvers/CMakeLists.txt:22);
+OpenMP mirrors the reference's `omp parallel for` loops (used when the CPU baseline is timed);
+no FMA contraction and no fast-math, so results are the same at any optimisation level and on
+x86-64 and aarch64 hosts.
 """
 from __future__ import annotations
 
@@ -24,7 +25,7 @@ def build_oracle(force: bool = False) -> pathlib.Path:
         return LIB
     cc = shutil.which("gcc") or "cc"
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [cc, "-std=c11", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", str(SRC), "-o", str(tmp), "-lm"]
+    cmd = [cc, "-std=c11", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", str(SRC), "-o", str(tmp), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{r.stderr}")

@@ -484,6 +484,21 @@ int ox_write_field(ox_sim* s, int comp, const double* in, size_t n) {
   return LX_OK;
 }
 
+/* Appends component `comp` to the file at `path` as its contiguous C-order doubles: the bytes
+ * fileio::writeHDF5 puts in one snapshot dataset (fileio.cc:186-201, H5T_NATIVE_DOUBLE,
+ * contiguous layout), without the HDF5 metadata.  Used to time the drivers' snapshot writes
+ * in the CPU baseline. */
+int ox_append_raw(ox_sim* s, int comp, const char* path) {
+  int sh[3];
+  if (ox_field_shape(s, comp, sh)) return LX_ERR_INVALID;
+  const size_t m = (size_t)sh[0] * sh[1] * sh[2];
+  FILE* f = fopen(path, "ab");
+  if (!f) return LX_ERR_IO;
+  const size_t w = m ? fwrite(comp_arr(s, comp)->a, sizeof(double), m, f) : 0;
+  if (fclose(f) != 0 || w != m) return LX_ERR_IO;
+  return LX_OK;
+}
+
 static arr3* cb_arr(ox_sim* s, int comp) {
   if (comp == LX_EX && !s->planar) return &s->Cb.x;
   if (comp == LX_EY) return &s->Cb.y;

@@ -41,6 +41,7 @@ def lib():
             ("ox_step", C.c_int, [C.c_void_p, C.c_int]),
             ("ox_add_dft_plane", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, P(C.c_double), C.c_int]),
             ("ox_read_dft", C.c_int, [C.c_void_p, C.c_int, P(C.c_double), C.c_size_t]),
+            ("ox_append_raw", C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -98,6 +99,10 @@ class OracleSim:
     def set_field(self, comp, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
         assert self.L.ox_write_field(self.h, comp, _dptr(a), a.size) == 0
+
+    def append_raw(self, comp, path):
+        """Appends the component's doubles to a file (the bytes of one snapshot dataset)."""
+        assert self.L.ox_append_raw(self.h, comp, str(path).encode()) == 0
 
     def set_cb(self, comp, cb):
         cb = np.ascontiguousarray(cb, dtype=np.float64)

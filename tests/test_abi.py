@@ -95,6 +95,45 @@ def test_yaml_fixture_2d(engine):
     assert p.usePML == 1 and p.d_pml == 0.02 and p.kappa == 5 and p.a_max == 0.05
 
 
+def test_reference_parameters_yaml_verbatim(engine):
+    """The reference's own parameters.yaml (byte-for-byte copy, UTF-8 BOM, comments and
+    trailing commas included) parses as reader::readYAML reads it (reader.cc:68-130) and
+    passes checkData: (1002 - 2) % 2 == 0 for the two x ranks (reader.cc:143-159)."""
+    from luxum_gb300 import read_yaml
+
+    raw = (GOLDEN / "reference_parameters.yaml").read_bytes()
+    assert raw.startswith(b"\xef\xbb\xbf")  # the verbatim file, BOM first
+    p = read_yaml(GOLDEN / "reference_parameters.yaml")
+    assert (p.isPlanar, p.Nx, p.Ny, p.Nz) == (1, 1002, 1, 1002)
+    assert (p.dx, p.dy, p.dz) == (0.001, 0.0, 0.001)
+    assert p.S == 0.70710678118 and p.num_timesteps == 2000
+    assert (p.npX, p.npY, p.n_threads) == (2, 1, 1)
+    assert (p.usePS, p.Nx_source, p.Ny_source, p.Nz_source, p.amp_source, p.omega_source) == (0, 0, 0, 0, 0, 0)
+    assert p.usePW == 1 and (p.kx_pw, p.ky_pw, p.kz_pw) == (0.70710678118, 0.0, 0.70710678118)
+    assert (p.Ex_pw, p.Ey_pw, p.Ez_pw, p.off_pw) == (0.0, 1.0, 0.0, 50.0)
+    assert (p.x1_pw, p.y1_pw, p.z1_pw, p.x2_pw, p.y2_pw, p.z2_pw) == (20, 20, 20, 980, 980, 980)
+    assert p.usePML == 0 and p.d_pml == 0.01 and p.sigma == 0.65 and p.sigma_m == 3
+    assert (p.kappa, p.a_max, p.a_m) == (15.0, 0.0, 1.0)
+    assert p.precision == 0 and p.cpml_mode == 0  # no engine-options document: reference behaviour
+
+
+def test_reference_parameters_3d_yaml_verbatim(engine):
+    """The reference's parameters_3d.yaml, verbatim: a 102^3 oblique plane wave with CPML on a
+    2 x 2 rank grid ((102 - 2) % 2 == 0 on both axes)."""
+    from luxum_gb300 import read_yaml
+
+    p = read_yaml(GOLDEN / "reference_parameters_3d.yaml")
+    assert (p.isPlanar, p.Nx, p.Ny, p.Nz) == (0, 102, 102, 102)
+    assert (p.dx, p.dy, p.dz) == (0.001, 0.001, 0.001)
+    assert p.S == 0.5773502691896258 and p.num_timesteps == 600
+    assert (p.npX, p.npY, p.n_threads) == (2, 2, 1)
+    assert p.usePW == 1 and p.kx_pw == p.ky_pw == p.kz_pw == 0.5773502691896258
+    assert (p.Ex_pw, p.Ey_pw, p.Ez_pw, p.off_pw) == (0.70710678118, 0.0, -0.70710678118, 0.0)
+    assert (p.x1_pw, p.y1_pw, p.z1_pw, p.x2_pw, p.y2_pw, p.z2_pw) == (20, 20, 20, 80, 80, 80)
+    assert p.usePML == 1 and p.d_pml == 0.01 and p.sigma == 0.65 and p.sigma_m == 3
+    assert (p.kappa, p.a_max, p.a_m) == (15.0, 0.0, 1.0)
+
+
 def test_yaml_fixture_3d_engine_options(engine):
     from luxum_gb300 import read_yaml
 

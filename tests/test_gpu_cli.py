@@ -85,3 +85,57 @@ def test_cli_missing_material_fails_unless_waived(engine, tmp_path):
     assert r.returncode != 0 and "airplane_100_x.h5" in r.stderr
     assert len(_run(tmp_path, "--no-material")) == 3
     assert (tmp_path / "Ez_data.h5").exists()
+
+
+def test_cli_reference_parameters_yaml(engine, tmp_path):
+    """The reference's own parameters.yaml, unmodified (byte-for-byte copy): solve_planar on
+    1002 x 1002 without CPML, an oblique TF/SF wave, 2000 steps, two x ranks in the file (one
+    GPU here).  Ey_data_2d.h5 holds Ey at t % 20 == 0 from t = 100 (two_dim.cc:140), and the
+    printed line of step t carries the max of step t itself (two_dim.cc:126-137).  Every
+    dataset is compared with the oracle at 1e-12."""
+    import os
+
+    from luxum_gb300 import EY, hdf5_read, read_yaml
+    from oracle.oracle import OracleSim
+
+    shutil.copy(GOLDEN / "reference_parameters.yaml", tmp_path / "parameters.yaml")
+    lines = _run(tmp_path)
+    p = read_yaml(tmp_path / "parameters.yaml")
+    assert [t for t, _ in lines] == list(range(2000))
+    o = OracleSim(p, threads=os.cpu_count() or 1)
+    checked = 0
+    for t in range(2000):
+        o.step(1)
+        assert lines[t][1] == pytest.approx(o.max_e2(), rel=1e-5, abs=1e-300), t
+        if t % 20 == 0 and t >= 100:
+            assert _close(hdf5_read(tmp_path / "Ey_data_2d.h5", f"t={t}")[:, 0, :], o.field(EY)[:, 0, :]), t
+            checked += 1
+    assert checked == 95 and lines[-1][1] > 0
+
+
+def test_cli_reference_parameters_3d_yaml(engine, tmp_path):
+    """The reference's parameters_3d.yaml, unmodified: solve3d_pml on 102^3 with an oblique
+    wave, 600 steps.  The airplane_100_*.h5 material files that driver reads are not in the
+    reference repository, so the run waives them (--no-material: vacuum, which is also what
+    the oracle runs).  |E|^2 goes to Ez_data.h5 every 3 steps (three_dim_pml.cc:279); one
+    dataset in 33 is compared with the oracle at 1e-12, and every printed max."""
+    import os
+
+    from luxum_gb300 import ETOTAL, hdf5_read, read_yaml
+    from oracle.oracle import OracleSim
+
+    shutil.copy(GOLDEN / "reference_parameters_3d.yaml", tmp_path / "parameters.yaml")
+    lines = _run(tmp_path, "--no-material")
+    p = read_yaml(tmp_path / "parameters.yaml")
+    assert [t for t, _ in lines] == list(range(600))
+    o = OracleSim(p, threads=os.cpu_count() or 1)
+    assert lines[0][1] == 0.0
+    checked = 0
+    for t in range(600):
+        o.step(1)
+        if t + 1 < 600:
+            assert lines[t + 1][1] == pytest.approx(o.max_e2(), rel=1e-5, abs=1e-300), t
+        if t % 99 == 0:
+            assert _close(hdf5_read(tmp_path / "Ez_data.h5", f"t={t}"), o.field(ETOTAL)), t
+            checked += 1
+    assert checked == 7 and o.max_e2() > 0

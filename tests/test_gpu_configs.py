@@ -1,0 +1,147 @@
+"""Parity at the benchmark configurations that run in float precision or at sizes the small
+cases do not reach, each against the FP64 oracle at the configuration's own grid size.
+
+- Photonic-crystal waveguide (512 x 512 x 128, eps_r 12 rods with a line defect, CPML 20,
+  pulsed Ez point source, FP64 DFT planes at x = 40 and x = 470): a 200-step FP64 window,
+  fields at 1e-12 and both planes' DFT accumulators at 1e-12.
+- Batch of planar lens simulations (FP32, 3000 steps, the first two members of the seeded
+  256-lens workload, stepped as one batch): every member's fields within 1e-4 relative L2
+  of the FP64 oracle (the FP32 form's stated bound).
+- Serving stream (FP32 fields, FP64 DFT at one monitor plane, 2000 steps): one 3-D and one
+  planar request of the seeded stream, served together, fields within 1e-4 and the monitor
+  flux within 1e-3 relative L2 of the FP64 oracle.
+
+Errors are relative L2 per component against its field group's norm (E or H), at the
+stated bound.  The per-component figure against the component's own norm is asserted too,
+where that norm is not cancellation noise (above 1e-6 of the group norm): 1e-9 for FP64 and
+1e-3 for FP32, since a small scattered component carries the absolute rounding error of the
+whole field in a smaller norm.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+THREADS = os.cpu_count() or 1
+
+
+def _check_fields(get_a, get_b, shapes, tol, own_tol=None):
+    """Group-normalised error per component <= tol; own-norm error <= own_tol where the
+    component carries more than 1e-6 of its group's norm.  Returns the figures."""
+    grp = cases.field_errors(get_a, get_b, shapes)
+    own = {}
+    for group in ((0, 1, 2), (3, 4, 5)):
+        comps = [c for c in group if np.prod(shapes[c]) > 0]
+        bs = {c: get_b(c) for c in comps}
+        gn = float(np.sqrt(sum(np.linalg.norm(b) ** 2 for b in bs.values())))
+        for c in comps:
+            nb = float(np.linalg.norm(bs[c]))
+            if gn > 0 and nb > 1e-6 * gn:
+                own[c] = float(np.linalg.norm(get_a(c) - bs[c])) / nb
+    for c, e in grp.items():
+        assert e <= tol, ("group-normalised", c, e, grp)
+    if own_tol is not None:
+        for c, e in own.items():
+            assert e <= own_tol, ("own-norm", c, e, own)
+    return grp, own
+
+
+def test_phc_fp64_window_vs_oracle(engine):
+    import bench
+    from oracle.oracle import OracleSim
+
+    g, (pin, pout) = bench.phc_sim(0)
+    o = OracleSim(bench.phc_params(0), threads=THREADS)
+    for lo, hi, eps in bench.phc_rods():
+        o.set_eps_box(lo, hi, eps)
+    oin = o.add_dft_plane(0, 40, bench.PHC_OMEGA, every=5)
+    oout = o.add_dft_plane(0, 470, bench.PHC_OMEGA, every=5)
+    g.step(200)
+    o.step(200)
+    shapes = {k: o.shape(k) for k in range(6)}
+    grp, own = _check_fields(g.field, o.field, shapes, 1e-12, 1e-9)
+    print("phc FP64 200 steps, group-normalised:", grp, "own-norm:", own)
+    a, b = g.dft(pin), o.dft(oin)
+    assert np.abs(b).max() > 0  # the pulse has reached the input plane
+    assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(b)
+    a, b = g.dft(pout), o.dft(oout)
+    assert np.array_equal(a, b)  # the wave has not reached the output plane: both exactly 0
+    assert g.max_e2() == pytest.approx(o.max_e2(), rel=1e-12)
+    g.close()
+    o.close()
+
+
+def test_lens_batch_members_fp32_vs_oracle(engine):
+    import bench
+    from luxum_gb300 import Batch, Sim
+    from oracle.oracle import OracleSim
+
+    steps = 3000
+    specs = bench.lens_specs(2, 4, 1, steps)  # an elliptic and a distorted lens
+    sims = []
+    batch = Batch(chunk=100)
+    for p, F in specs:
+        s = Sim(p)
+        s.set_material(1, F, 1.0)
+        batch.add(s)
+        sims.append(s)
+    batch.step(steps)
+    for (p, F), s in zip(specs, sims):
+        o = OracleSim(p, threads=THREADS)  # the oracle runs FP64 whatever the precision field says
+        o.set_material(1, F, 1.0)
+        o.step(steps)
+        shapes = {k: o.shape(k) for k in range(6)}
+        grp, own = _check_fields(s.field, o.field, shapes, 1e-4, 1e-3)
+        print(f"lens member {p.Nx}^2 FP32 batched, {steps} steps: group-normalised", grp, "own-norm", own)
+        assert s.t == steps
+        o.close()
+    batch.close()
+
+
+def test_served_requests_fp32_vs_oracle(engine):
+    import bench
+    from luxum_gb300 import Server
+    from oracle.oracle import OracleSim
+
+    reqs = bench.serve_requests(1000, 5, 50.0)
+    pick = [reqs[9], reqs[0]]  # the stream's first 3-D request of side >= 100, and its first request
+    assert not pick[0]["planar"] and pick[1]["planar"]
+    steps = bench.SERVE_STEPS
+    with Server(precision=1, chunk=100) as srv:
+        ids = []
+        for r in pick:
+            plane = r["side"] - 1 - 2 * bench.serve_margin(r["side"]) - 4
+            ids.append(srv.submit(bench.serve_params(r), steps, r["boxes"], (0, plane, bench.SERVE_OMEGA, 10)))
+        for rid in ids:
+            assert srv.wait(rid, 600.0) == "done", srv.error(rid)
+        for rid, r in zip(ids, pick):
+            p = bench.serve_params(r)
+            fg = srv.flux(rid)
+            g = srv.take(rid, p)
+            p0 = bench.serve_params(r)
+            p0.precision = 0
+            o = OracleSim(p0, threads=THREADS)
+            for lo, hi, eps in r["boxes"]:
+                o.set_eps_box(lo, hi, eps)
+            plane = r["side"] - 1 - 2 * bench.serve_margin(r["side"]) - 4
+            od = o.add_dft_plane(0, plane, bench.SERVE_OMEGA, every=10)
+            o.step(steps)
+            shapes = {k: o.shape(k) for k in range(6)}
+            grp, own = _check_fields(g.field, o.field, shapes, 1e-4, 1e-3)
+            acc = o.dft(od)  # (nfreq, 4, na, nb): Ey, Ez, Hy, Hz on an x plane
+            dA = p0.dy * p0.dz if not r["planar"] else p0.dz
+            fo = np.real(acc[:, 0] * np.conj(acc[:, 3]) - acc[:, 1] * np.conj(acc[:, 2])).sum(axis=(1, 2)) * dA
+            ferr = float(np.linalg.norm(fg - fo) / np.linalg.norm(fo))
+            assert ferr <= 1e-3, ferr
+            print(f"served {'planar' if r['planar'] else '3-D'} side {r['side']} FP32, {steps} steps: "
+                  f"group-normalised {grp}, own-norm {own}, flux rel-L2 {ferr:.2e}")
+            o.close()
+            g.close()

@@ -67,6 +67,49 @@ def test_server_results_equal_solo(engine):
         assert st["cell_updates"] > 0 and st["bytes_running"] == pytest.approx(0.0, abs=1.0)
 
 
+def test_server_arrivals_while_others_run(engine):
+    """Continuous batching: A and B are submitted first; C and D arrive once A is running and
+    at least one chunk has finished, and join the batch between chunks while A and B are still
+    on the GPU.  Every request must still equal its twin stepped alone, bit for bit (fields,
+    flux and max|E|^2)."""
+    import time
+
+    from luxum_gb300 import Server
+
+    first = [("3d_pml_axis", 3000, [((12, 10, 12), (18, 16, 20), 6.0)], (0, 20, W, 2)),
+             ("planar_pml_axis", 2000, [((20, 0, 20), (30, 1, 40), 4.0)], (0, 45, W, 1))]
+    late = [("planar_oblique", 150, [], (2, 28, W, 5)),
+            ("3d_oblique", 90, [((10, 10, 10), (14, 20, 16), 2.5)], None)]
+    with Server(chunk=20) as srv:
+        ids = [srv.submit(_params(n), steps, boxes, dft) for n, steps, boxes, dft in first]
+        t0 = time.monotonic()
+        while not (srv.state(ids[0]) == "running" and srv.stats()["chunks"] >= 1):
+            assert time.monotonic() - t0 < 60.0
+            srv.wait(ids[0], 0.002)
+        assert srv.state(ids[0]) == "running"  # A is mid-run when C and D arrive
+        ids += [srv.submit(_params(n), steps, boxes, dft) for n, steps, boxes, dft in late]
+        for rid in ids:
+            assert srv.wait(rid, 120.0) == "done", srv.error(rid)
+        ta = srv.times(ids[0])
+        for rid in ids[2:]:
+            tc = srv.times(rid)
+            assert tc[0] > ta[1]  # submitted after A had started
+        # at least one late request ran while A was still running
+        assert min(srv.times(rid)[1] for rid in ids[2:]) < ta[2]
+        for rid, (n, steps, boxes, dft) in zip(ids, first + late):
+            twin, plane = _solo(n, steps, boxes, dft)
+            if dft is not None:
+                assert np.array_equal(srv.flux(rid), twin.dft_flux(plane)), n
+            assert srv.max_e2(rid) == twin.max_e2(), n
+            g = srv.take(rid, _params(n))
+            assert g.t == steps
+            for c in range(6):
+                if np.prod(g.shape(c)):
+                    assert np.array_equal(g.field(c), twin.field(c)), (n, c)
+            g.close()
+            twin.close()
+
+
 def test_server_budget_and_cancel(engine):
     from luxum_gb300 import Server, device_bytes
 

@@ -24,8 +24,9 @@ def _read_noalloc(sim, comp):
     return out
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_noalloc_read_matches_read_field(engine, precision):
+    """3-D handle in FP64, FP32 and FP16 storage (H stored scaled, read back unscaled)."""
     from luxum_gb300 import Sim
 
     p, steps, boxes = cases.build("3d_pml_axis")
@@ -42,6 +43,28 @@ def test_noalloc_read_matches_read_field(engine, precision):
         second = _read_noalloc(sim, comp)
         assert np.array_equal(first, ref), comp
         assert np.array_equal(second, ref), comp
+        assert np.any(ref != 0), comp
+    sim.close()
+
+
+@pytest.mark.parametrize("steps", [37, 38])
+def test_noalloc_read_planar_two_buffer_state(engine, steps):
+    """A planar FP32 handle stepped alone keeps its state in two buffers and, after an odd
+    number of steps, in the second one: the read must pick the same buffer as the
+    allocating read."""
+    from luxum_gb300 import Sim
+
+    p, _, boxes = cases.build("planar_pml_axis")
+    p.precision = 1
+    sim = Sim(p)
+    for lo, hi, eps in boxes:
+        sim.set_eps_box(lo, hi, eps)
+    sim.step(steps)
+    sim.sync()
+    for comp in (1, 3, 5):  # Ey, Hx, Hz: the planar components
+        ref = sim.field(comp)
+        for _ in range(2):
+            assert np.array_equal(_read_noalloc(sim, comp), ref), comp
         assert np.any(ref != 0), comp
     sim.close()
 
