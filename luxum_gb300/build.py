@@ -19,7 +19,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libluxum.so"
 CLI = PKG / "luxum"
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["lx_kernels.cu", "lx_api.cu", "lx_yaml.cpp", "lx_hdf5.cpp", "lx_noalloc.cu", "lx_server.cpp"]
+LIB_SOURCES = ["lx_kernels.cu", "lx_sweep3d.cu", "lx_api.cu", "lx_yaml.cpp", "lx_hdf5.cpp", "lx_noalloc.cu", "lx_server.cpp"]
 
 
 def nvcc() -> str:
@@ -30,7 +30,7 @@ def nvcc() -> str:
 
 
 def _deps() -> list[pathlib.Path]:
-    return sorted(CSRC.glob("*.h")) + [REPO / "include" / "luxum.h", pathlib.Path(__file__)]
+    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [REPO / "include" / "luxum.h", pathlib.Path(__file__)]
 
 
 def _stale(out: pathlib.Path, srcs: list[pathlib.Path]) -> bool:

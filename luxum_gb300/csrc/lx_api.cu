@@ -495,6 +495,7 @@ static lx_status create_typed(lx_sim* s) {
   }
   CK(cudaMallocAsync(&s->d_max, 64, s->own));
   CK(cudaMemsetAsync(s->d_max, 0, 64, s->own));
+  s->d_fault = reinterpret_cast<unsigned*>(s->d_max + 1);
   return LX_OK;
 }
 
@@ -517,11 +518,15 @@ static void setup_host(lx_sim* s, const lx_params* p) {
   s->ncell = (size_t)s->Nx * s->Ny * s->Nzp;
   compute_extents(s);
   // Planar handles with float compute step in one sweep over two state buffers; FP64 is bound
-  // by the FP64 pipe, where the sweep's recomputed halo would only add work.  LUXUM_TWO_SWEEP=1
-  // in the environment keeps new handles on the in-place two-sweep kernels (A/B checks).
+  // by the FP64 pipe, where the sweep's recomputed halos would only add work.  3-D float
+  // handles take the single-sweep kernel (lx_sweep3d.cu) when LUXUM_SWEEP3=1: it runs ahead
+  // of the two-sweep kernels on grids without CPML and TF/SF and behind them with both.
+  // LUXUM_TWO_SWEEP=1 keeps new handles on the in-place two-sweep kernels (A/B checks).
   {
     const char* two = std::getenv("LUXUM_TWO_SWEEP");
-    s->sweep = s->planar && p->precision != LX_PREC_FP64 && !(two && two[0] == '1');
+    const char* s3 = std::getenv("LUXUM_SWEEP3");
+    s->sweep = p->precision != LX_PREC_FP64 && !(two && two[0] == '1') &&
+               (s->planar || (s3 && s3[0] == '1'));
   }
 
   // maxwell::maxwell maxwell.cc:60-148
@@ -1489,6 +1494,7 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
     if (st) return st;
   }
   lx::StepParams<T, C> sp = step_params<T, C>(s);
+  sp.fault = s->d_fault;
   lx::PrologueParams pp = make_prologue(s);
   T* pf[6];  // the components after the current step (buffer (t+1) & 1 in ping-pong mode)
   auto post_step = [&](int t) {
@@ -1553,7 +1559,8 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
         lx::StepParams<T, C> sw = sp;
         if (t & 1) swap_buffers(sw);
         if ((st = tic())) return st;
-        CK(lx::launch_step_sweep2<T, C>(sw, s->uniform, s->stream));
+        if (s->planar) CK(lx::launch_step_sweep2<T, C>(sw, s->uniform, s->stream));
+        else CK(lx::launch_step_sweep3<T, C>(sw, s->uniform, s->stream));
         if ((st = toc(1))) return st;
         s->n_kernels += 1;
         swept = true;
@@ -1599,9 +1606,15 @@ static lx_status run_steps(lx_sim* s, int nsteps, KernelTimer* kt = nullptr) {
   }
   if (nsteps > 0) {
     unsigned long long bits = 0;
+    unsigned fault = 0;
     CK(cudaMemcpyAsync(&bits, last_slot, sizeof bits, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(&fault, s->d_fault, sizeof fault, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    s->n_d2h += sizeof bits;
+    s->n_d2h += sizeof bits + sizeof fault;
+    if (fault) {
+      CK(cudaMemsetAsync(s->d_fault, 0, sizeof fault, s->stream));
+      return fail(s, LX_ERR_CUDA, "a sweep kernel's bounded wait for a staged plane ran out; the step's fields are not valid");
+    }
     double v;
     std::memcpy(&v, &bits, sizeof v);
     s->last_max = v;

@@ -130,6 +130,8 @@ struct StepParams {
   // Set by the single-simulation 3-D launch: 1 when a block's z tile 0 is the row's two
   // 16-cell ends (see ZTile in lx_kernels.cu), 0 for plain 32-cell tiles.
   int zends;
+  // Set to nonzero by a kernel whose bounded wait for staged data ran out (null: not reported).
+  unsigned* fault;
 };
 
 // Whether a block's tile [i0,i0+ni) x [j0,j0+nj) x [k0,k0+nk) meets any TF/SF plane of the

@@ -14,6 +14,10 @@ cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bo
 // p.E, p.H, p.psiH, p.psiE and writes those in p.E1, p.H1, p.psiH1, p.psiE1.
 template <class T, class C>
 cudaError_t launch_step_sweep2(const StepParams<T, C>& p, bool uniform, cudaStream_t s);
+// Single-sweep 3-D step (float compute, two state buffers), lx_sweep3d.cu: the same buffer
+// convention as launch_step_sweep2.
+template <class T, class C>
+cudaError_t launch_step_sweep3(const StepParams<T, C>& p, bool uniform, cudaStream_t s);
 template <class T>
 cudaError_t launch_gather(const T* src, double* dst, const int ext[3], int Ny, int Nzp, double mul, cudaStream_t s);
 template <class T>

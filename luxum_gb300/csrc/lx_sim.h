@@ -101,7 +101,7 @@ struct lx_sim {
   void* prof[3][6] = {};  // per axis: bE cE rkE bH cH rkH (compute precision)
   void* psiH[3][2] = {};
   void* psiE[3][2] = {};
-  // Single-sweep handles (planar, float compute) keep a second copy of the state.  Stepped
+  // Single-sweep handles (float compute) keep a second copy of the state.  Stepped
   // alone they run in ping-pong mode (pp): after t steps the state lives in buffer t & 1
   // (buffer 0 = E, H, psiH, psiE above, buffer 1 here).  In a batch they are updated in place
   // in buffer 0 (pp = 0); set_pp moves the state when the mode changes.
@@ -117,6 +117,7 @@ struct lx_sim {
   int tab_total = 0;
   lx::PatchSet setsH[3][2] = {}, setsE[3][2] = {};
   unsigned long long* d_max = nullptr;
+  unsigned* d_fault = nullptr;  // in d_max's allocation: set by a kernel whose bounded wait ran out
   // max|E|^2 series: one slot per monitored step (device), the step of each slot (host)
   unsigned long long* d_series = nullptr;
   int series_cap = 0;

@@ -193,8 +193,9 @@ def test_ctypes_structs_match_the_header(tmp_path):
 @pytest.mark.parametrize("precision,two_buffers", [(0, False), (1, True), (2, True)])
 def test_device_bytes_counts_the_second_state_buffer(engine, monkeypatch, precision, two_buffers):
     """Planar FP32 / FP16-storage handles keep two copies of E, H and psi (the single-sweep
-    step); lx_params_device_bytes, which the server admits requests by, counts both.  3-D and
-    FP64 handles keep one.  LUXUM_TWO_SWEEP=1 keeps new planar float handles at one copy."""
+    step), and so do 3-D ones with LUXUM_SWEEP3=1; lx_params_device_bytes, which the server
+    admits requests by, counts both.  FP64 handles keep one.  LUXUM_TWO_SWEEP=1 keeps new float
+    handles at one copy."""
     from luxum_gb300 import device_bytes, field_shape
 
     kw = dict(isPlanar=1, Nx=300, Ny=1, Nz=520, precision=precision, **cases.pml(16))
@@ -215,8 +216,14 @@ def test_device_bytes_counts_the_second_state_buffer(engine, monkeypatch, precis
     per_cell_of_width = (2 * nzp + 2 * 300) * 4
     psi = both - one - fields
     assert psi % per_cell_of_width == 0 and 16 <= psi // per_cell_of_width <= 32
+    # 3-D: one copy, unless the single-sweep kernel is asked for (then a second copy of the six
+    # components; no CPML here)
     p3 = cases.make(isPlanar=0, Nx=40, Ny=40, Nz=40, precision=precision)
     monkeypatch.delenv("LUXUM_TWO_SWEEP", raising=False)
-    a = device_bytes(p3)
+    monkeypatch.delenv("LUXUM_SWEEP3", raising=False)
+    one3 = device_bytes(p3)
+    monkeypatch.setenv("LUXUM_SWEEP3", "1")
+    nzp3 = -(-40 * tsize // 128) * 128 // tsize
+    assert device_bytes(p3) - one3 == 6 * 40 * 40 * nzp3 * tsize
     monkeypatch.setenv("LUXUM_TWO_SWEEP", "1")
-    assert device_bytes(p3) == a
+    assert device_bytes(p3) == one3

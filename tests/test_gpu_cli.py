@@ -118,7 +118,13 @@ def test_cli_reference_parameters_3d_yaml(engine, tmp_path):
     wave, 600 steps.  The airplane_100_*.h5 material files that driver reads are not in the
     reference repository, so the run waives them (--no-material: vacuum, which is also what
     the oracle runs).  |E|^2 goes to Ez_data.h5 every 3 steps (three_dim_pml.cc:279); one
-    dataset in 33 is compared with the oracle at 1e-12, and every printed max."""
+    dataset in 33 is compared with the oracle, and every printed max.
+
+    The file runs at the 3-D Courant limit (S = 1/sqrt 3) in vacuum: once the pulse has left
+    the total-field box (t ~ 280), |E|^2 is only the box faces' cancellation residue, some
+    1e-3 of its peak, and the relative error of that residue is no measure of the update.  So
+    each dataset's difference is bounded by 1e-12 of the largest |E|^2 norm the run has had
+    so far; up to t = 264 that is also 1e-12 of the dataset's own norm, and is checked too."""
     import os
 
     from luxum_gb300 import ETOTAL, hdf5_read, read_yaml
@@ -130,12 +136,17 @@ def test_cli_reference_parameters_3d_yaml(engine, tmp_path):
     assert [t for t, _ in lines] == list(range(600))
     o = OracleSim(p, threads=os.cpu_count() or 1)
     assert lines[0][1] == 0.0
-    checked = 0
+    checked, peak = 0, 0.0
     for t in range(600):
         o.step(1)
         if t + 1 < 600:
             assert lines[t + 1][1] == pytest.approx(o.max_e2(), rel=1e-5, abs=1e-300), t
-        if t % 99 == 0:
-            assert _close(hdf5_read(tmp_path / "Ez_data.h5", f"t={t}"), o.field(ETOTAL)), t
+        if t % 33 == 0:
+            a, b = hdf5_read(tmp_path / "Ez_data.h5", f"t={t}"), o.field(ETOTAL)
+            peak = max(peak, float(np.linalg.norm(b)))
+            d = float(np.linalg.norm(a - b))
+            assert d <= 1e-12 * peak, (t, d / peak)
+            if t <= 264:
+                assert _close(a, b), t
             checked += 1
-    assert checked == 7 and o.max_e2() > 0
+    assert checked == 19 and o.max_e2() > 0

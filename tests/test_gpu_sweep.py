@@ -1,7 +1,7 @@
-"""Single-sweep planar step against the two-sweep kernels.
+"""Single-sweep steps (planar and 3-D) against the two-sweep kernels.
 
-Planar handles with float compute (FP32 and FP16 storage) form H and E of a step in one
-launch over two state buffers: state n is read from one and state n+1 written to the other.
+Handles with float compute (FP32 and FP16 storage) form H and E of a step in one launch
+over two state buffers: state n is read from one and state n+1 written to the other.
 Handles created while LUXUM_TWO_SWEEP=1 is set use the in-place two-sweep kernels instead.
 Both must give the same fields, DFT accumulators, probe series and max|E|^2 series, bit for
 bit: at odd and even step counts, through a checkpoint written at an odd step, and across
@@ -51,7 +51,11 @@ def _sim(p, boxes, dft=True):
 def _pair(p, boxes, dft=True):
     """(single-sweep handle, two-sweep handle) of the same parameters."""
     os.environ.pop("LUXUM_TWO_SWEEP", None)
-    a = _sim(p, boxes, dft)
+    os.environ["LUXUM_SWEEP3"] = "1"  # 3-D float handles too
+    try:
+        a = _sim(p, boxes, dft)
+    finally:
+        del os.environ["LUXUM_SWEEP3"]
     os.environ["LUXUM_TWO_SWEEP"] = "1"
     try:
         b = _sim(p, boxes, dft)
@@ -64,15 +68,17 @@ def _pair(p, boxes, dft=True):
 
 def _same(a, b):
     assert a.t == b.t
-    for c in (1, 3, 5):  # Ey, Hx, Hz
-        assert np.array_equal(a.field(c), b.field(c)), (a.t, c)
+    for c in range(6):  # the planar grids hold Ey, Hx, Hz only
+        if np.prod(a.shape(c)):
+            assert np.array_equal(a.field(c), b.field(c)), (a.t, c)
     for plane in getattr(a, "_dft", {}):
         assert np.array_equal(a.dft(plane), b.dft(plane)), a.t
     assert a.max_e2() == b.max_e2()
 
 
 @pytest.mark.parametrize("precision", [1, 2])
-@pytest.mark.parametrize("name", ["planar_pml_axis", "planar_oblique", "planar_pml_std_oblique"])
+@pytest.mark.parametrize("name", ["planar_pml_axis", "planar_oblique", "planar_pml_std_oblique", "3d_pml_axis",
+                                  "3d_oblique", "3d_pml_y_amax", "3d_pml_point_cw", "3d_pml_pulse_nonuniform"])
 def test_sweep_equals_two_sweep_small(engine, name, precision):
     a, b = _pair(*_small(name, precision))
     for n in (1, 36, 1, 2, 17):  # odd and even step counts
@@ -166,4 +172,92 @@ def test_sweep_handles_in_a_batch(engine, precision):
     for a, b in pairs:
         a.step(6)
         b.step(6)
+        _same(a, b)
+
+
+def _big3(precision, uniform=True, n=(256, 128, 160)):
+    """A 3-D grid with every tile kind of the 3-D sweep: interior tiles, tiles in the CPML
+    slabs and on the TF/SF faces, partial tiles at the y and z ends, and (at the default
+    size) 16 planes per block."""
+    nx, ny, nz = n
+    mx, my, mz = (min(20, v // 3) for v in n)  # TF/SF faces inside the 10-cell CPML
+    kw = dict(isPlanar=0, Nx=nx, Ny=ny, Nz=nz,
+              **cases.pw((1, 0, 0), (0, 0, 1), ((mx, nx - 1 - mx), (my, ny - 1 - my), (mz, nz - 1 - mz))),
+              **cases.pml(10, kappa=5.0, a_max=0.05), usePS=1, source_kind=1, Nx_source=nx // 2, Ny_source=ny // 2,
+              Nz_source=nz // 2, amp_source=1.0, omega_source=2.0e11, src_t0=15.0, src_tw=6.0, precision=precision)
+    if not uniform:
+        kw["dy"] = 1.25e-3
+    boxes = [((nx // 3, ny // 3, nz // 3), (nx // 2, ny // 2 + 7, nz // 2 + 3), 4.0)]
+    return cases.make(**kw), boxes
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("uniform, n", [(True, (256, 128, 160)), (False, (90, 75, 101)), (True, (33, 200, 47))])
+def test_sweep3_equals_two_sweep_large(engine, precision, uniform, n):
+    p, boxes = _big3(precision, uniform, n)
+    a, b = _pair(p, boxes)
+    nx, ny, nz = n
+    ijk = np.array([[nx // 2, ny // 2, nz // 2], [5, 6, 7], [nx - 2, ny - 2, nz - 2], [nx // 3, 1, nz - 1]],
+                   dtype=np.int32)
+    for s in (a, b):
+        s.set_probes(ijk, 200)
+        s.set_max_series(200)
+    a.step(41)
+    b.step(41)
+    _same(a, b)
+    a.step(30)
+    b.step(30)
+    _same(a, b)
+    assert np.array_equal(a.probes(), b.probes())
+    ta, va = a.max_series()
+    tb, vb = b.max_series()
+    assert np.array_equal(ta, tb) and np.array_equal(va, vb)
+    assert a.max_e2() > 0
+
+
+def test_sweep3_etotal_snapshot_and_checkpoint(engine, tmp_path):
+    """|E|^2 snapshots from the 3-D sweep, and a checkpoint written at an odd step."""
+    p, boxes = _big3(1, True, (90, 75, 101))
+    a, b = _pair(p, boxes, dft=False)
+    got = {}
+    for s, key in ((a, "a"), (b, "b")):
+        s.set_snapshots(7, 1 << 6, lambda t, c, arr, key=key: got.setdefault((key, t), np.array(arr)))
+    a.step(29)
+    b.step(29)
+    a.sync()
+    b.sync()
+    for t in (0, 7, 14, 21, 28):
+        assert np.array_equal(got[("a", t)], got[("b", t)]), t
+    path = str(tmp_path / "odd3.h5")
+    a.save(path)
+    c = _sim(p, boxes, dft=False)
+    c.load(path)
+    for s in (a, b, c):
+        s.step(12)
+    _same(a, b)
+    _same(c, b)
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_sweep3_handles_in_a_batch(engine, precision):
+    """3-D single-sweep handles join a batch at odd and even steps and leave it again."""
+    from luxum_gb300 import Batch
+
+    specs = [_small("3d_pml_axis", precision), _small("3d_oblique", precision), _big3(precision, True, (90, 75, 101))]
+    pairs = [_pair(p, boxes) for p, boxes in specs]
+    for k, (a, b) in enumerate(pairs):
+        a.step(3 + k)
+        b.step(3 + k)
+    batch = Batch(chunk=10)
+    for a, _ in pairs:
+        batch.add(a)
+    batch.step(25)
+    for _, b in pairs:
+        b.step(25)
+    for a, b in pairs:
+        _same(a, b)
+    batch.remove(pairs[2][0])
+    for a, b in pairs:
+        a.step(5)
+        b.step(5)
         _same(a, b)
