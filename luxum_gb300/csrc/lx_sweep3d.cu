@@ -47,7 +47,7 @@ namespace {
 constexpr int kTY = 8;                    // rows (y) per block, one warp each
 constexpr int kStages = 4;                // planes in flight per block
 constexpr int kThreads = 32 * (kTY + 1);  // the row warps and one halo / producer warp
-constexpr long long kSpin = 1LL << 20;    // bound of a wait on a staged plane (normally a few hundred tries)
+constexpr long long kSpin = 1LL << 20;    // bound of the tries of a wait on a staged plane (normally a few)
 
 // ---- the arithmetic of h_apply for the H of a cell of another block (three_dim_pml.cc:176-213)
 
@@ -146,14 +146,17 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned b
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
 }
 // Waits, with a bound, for the phase of the given parity to complete; false when the bound ran out.
+// Each try may suspend the warp for up to kSuspendNs instead of returning at once, so a waiting
+// warp does not take issue slots from the warps that are computing.
+constexpr unsigned kSuspendNs = 1000;
 __device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity) {
   const unsigned a = smem_u32(b);
   for (long long it = 0; it < kSpin; ++it) {
     unsigned ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(kSuspendNs)
         : "memory");
     if (ok) return true;
   }

@@ -152,8 +152,14 @@ def test_served_requests_fp32_vs_oracle(engine):
             acc = o.dft(od)  # (nfreq, 4, na, nb): Ey, Ez, Hy, Hz on an x plane
             dA = p0.dy * p0.dz if not r["planar"] else p0.dz
             fo = np.real(acc[:, 0] * np.conj(acc[:, 3]) - acc[:, 1] * np.conj(acc[:, 2])).sum(axis=(1, 2)) * dA
-            ferr = float(np.linalg.norm(fg - fo) / np.linalg.norm(fo))
-            assert ferr <= 1e-3, ferr
+            if np.linalg.norm(fo) == 0.0:
+                # the pulse has not reached the plane in 2000 steps (the planar request's plane
+                # lies 1670 cells downstream): both sides hold exact zeros
+                assert np.array_equal(fg, fo)
+                ferr = 0.0
+            else:
+                ferr = float(np.linalg.norm(fg - fo) / np.linalg.norm(fo))
+                assert ferr <= 1e-3, ferr
             print(f"served {'planar' if r['planar'] else '3-D'} side {r['side']} FP32, {steps} steps: "
                   f"group-normalised {grp}, own-norm {own}, flux rel-L2 {ferr:.2e}")
             o.close()
