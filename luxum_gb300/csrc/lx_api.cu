@@ -1778,14 +1778,19 @@ struct lx_batch {
   cudaStream_t stream = nullptr;
   // 3-D members of at least kSoloCells cells take one kernel pair each, with their parameter
   // block passed by value (the constant bank, as for a handle stepped alone), spread over the
-  // batch stream and kLanes - 1 more so that the members' kernels overlap.
+  // batch stream and kLanes - 1 more so that the members' kernels overlap.  Planar members with
+  // float compute of at least kSoloCells2 cells take the single-sweep kernel the same way, in
+  // their two buffers (ping-pong mode); smaller members share the batched launches in place.
   static constexpr long long kSoloCells = 1LL << 18;
+  // (2^21 cells: a member's sweep takes ~15 us; at 2^18 the launches of the 256-lens batch's
+  // larger half cost more than the single sweep saves, 103 -> 96 Gcell/s)
+  static constexpr long long kSoloCells2 = 1LL << 21;
   static constexpr int kLanes = 4;
   cudaStream_t lanes[kLanes - 1] = {};
   cudaEvent_t lane_ev[kLanes] = {};  // [0] fork, [1..] joins
   struct Group {  // members sharing (planar, uniform, solo): one update launch per half step
     bool planar = false, uniform = false;
-    bool solo = false;              // 3-D members launched one by one (kSoloCells and larger)
+    bool solo = false;              // members launched one by one (kSoloCells / kSoloCells2 and larger)
     std::vector<char> host_params;  // solo groups: the members' parameter blocks
     int march = lx::kMarch3;   // cells each thread walks along x
     std::vector<int> members;  // batch-global indices
@@ -1918,7 +1923,6 @@ extern "C" LX_API lx_status lx_batch_add(lx_batch* b, lx_sim* s) {
   if (!s->outputs.empty() || s->nprobes > 0 || s->d_series)
     return bfail(b, LX_ERR_UNSUPPORTED, "batched members cannot have snapshot outputs, probes or a max series");
   if ((st = lx_sim_sync(s))) return st;
-  if ((st = set_pp(s, false))) return st;  // batches update their members in place
   b->prec = s->prec;
   b->sims.push_back(s);
   s->batch = b;
@@ -1952,6 +1956,15 @@ static lx_status batch_rebuild(lx_batch* b) {
   b->graphable = true;
   BCK(cudaMallocAsync(&b->d_slots, sizeof(unsigned long long) * (n > 0 ? n : 1), b->stream));
   std::vector<std::vector<lx::DftParams>> dft_planes;
+  // Large planar single-sweep members step in their two buffers, the others in place in buffer 0;
+  // a member whose mode changes at an odd step moves its state (one device copy).
+  for (int q = 0; q < n; q++) {
+    lx_sim* s = b->sims[q];
+    const bool two = s->sweep && s->planar && (long long)s->Nx * s->Nz >= lx_batch::kSoloCells2;
+    lx_status st;
+    if ((st = set_pp(s, two))) return st;
+    BCK(cudaStreamSynchronize(s->stream));
+  }
   for (int q = 0; q < n; q++) {
     lx_sim* s = b->sims[q];
     pps[q] = make_prologue(s);
@@ -1965,8 +1978,10 @@ static lx_status batch_rebuild(lx_batch* b) {
       dp.axis = d.axis; dp.index = d.index; dp.na = d.na; dp.nb = d.nb; dp.Ny = s->Ny; dp.Nzp = s->Nzp;
       dp.nfreq = d.nfreq; dp.dt = s->k.dt; dp.weight = (double)d.every; dp.every_ = d.every;
       dp.omega = d.d_omega; dp.acc = d.d_acc; dp.phase = d.d_phase; dp.sim = q; dp.hmul = 1.0 / s->hscale;
+      T* pf1[6] = {(T*)s->E1[0], (T*)s->E1[1], (T*)s->E1[2], (T*)s->H1[0], (T*)s->H1[1], (T*)s->H1[2]};
       for (int c = 0; c < 4; c++) {
         dp.f[c] = pf[d.comps[c]];
+        dp.f1[c] = s->pp ? pf1[d.comps[c]] : nullptr;
         for (int a = 0; a < 3; a++) dp.ext[c][a] = s->ext[d.comps[c]][a];
       }
       // sampled at batch steps b' with (t + b' - step) % every == 0
@@ -1984,7 +1999,8 @@ static lx_status batch_rebuild(lx_batch* b) {
       dft_planes[ci].push_back(dp);
       if (b->chunk > 0 && b->chunk % d.every != 0) b->graphable = false;
     }
-    const bool solo = !s->planar && (long long)s->Nx * s->Ny * s->Nz >= lx_batch::kSoloCells;
+    const bool solo = s->pp || (!s->planar && (long long)s->Nx * s->Ny * s->Nz >= lx_batch::kSoloCells);
+    if (s->pp && b->chunk % 2) b->graphable = false;  // a captured chunk must keep each member's parity
     int gi = -1;
     for (size_t g = 0; g < b->groups.size(); g++)
       if (b->groups[g].planar == (bool)s->planar && b->groups[g].uniform == (bool)s->uniform &&
@@ -2063,8 +2079,16 @@ static lx_status batch_enqueue(lx_batch* b, long long step0, int nsteps) {
         for (int l = 0; l < L - 1; l++) BCK(cudaStreamWaitEvent(b->lanes[l], b->lane_ev[0], 0));
         for (size_t m = 0; m < g.members.size(); m++) {
           cudaStream_t st = (m % L) ? b->lanes[m % L - 1] : b->stream;
-          BCK(lx::launch_step<T, C>(hp[m], false, g.uniform, true, st));
-          BCK(lx::launch_step<T, C>(hp[m], false, g.uniform, false, st));
+          if constexpr (sizeof(C) == 4) {
+            if (g.planar) {  // single sweep, state t & 1 -> (t+1) & 1
+              lx::StepParams<T, C> sw = hp[m];
+              if ((b->host_ts[g.members[m]] + q) & 1) swap_buffers(sw);
+              BCK(lx::launch_step_sweep2<T, C>(sw, g.uniform, st));
+              continue;
+            }
+          }
+          BCK(lx::launch_step<T, C>(hp[m], g.planar, g.uniform, true, st));
+          BCK(lx::launch_step<T, C>(hp[m], g.planar, g.uniform, false, st));
         }
         for (int l = 0; l < L - 1; l++) {
           BCK(cudaEventRecord(b->lane_ev[1 + l], b->lanes[l]));

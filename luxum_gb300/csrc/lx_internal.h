@@ -176,6 +176,8 @@ struct DftParams {
   int axis, index, na, nb, Ny, Nzp, nfreq, t;
   int sim;                // batched launches: index of the simulation's step counter
   const void* f[4];       // batched launches: the four sampled components
+  const void* f1[4];      // ... in buffer 1, for members stepped in two buffers (null otherwise):
+                          // the state after step t lives in buffer (t + 1) & 1
   int ext[4][3];          // extents of the four sampled components
   double dt, weight;
   double hmul;            // 1/hscale for the two H components

@@ -1086,7 +1086,8 @@ __global__ void dft_batch_kernel(const DftParams* __restrict__ ds, const int2* _
   const DftParams& d = ds[bm.x];
   const int t = ts[d.sim] + k;
   if (t % d.every_ != 0) return;
-  dft_body<T>(d, (const T*)d.f[0], (const T*)d.f[1], (const T*)d.f[2], (const T*)d.f[3], bm.y);
+  const void* const* f = (d.f1[0] || d.f1[1]) && ((t + 1) & 1) ? d.f1 : d.f;  // the state after step t
+  dft_body<T>(d, (const T*)f[0], (const T*)f[1], (const T*)f[2], (const T*)f[3], bm.y);
 }
 
 // Net flux of a DFT plane per frequency: partial sums over fixed chunks of 1024 cells, then

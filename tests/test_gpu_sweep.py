@@ -261,3 +261,35 @@ def test_sweep3_handles_in_a_batch(engine, precision):
         a.step(5)
         b.step(5)
         _same(a, b)
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_large_planar_member_steps_in_two_buffers(engine, precision):
+    """A planar member of 2^21 cells or more takes the single-sweep kernel inside a batch, by
+    value and in its two buffers, with its DFT plane read from the buffer of each step's
+    parity; it must equal the same simulation on the two-sweep kernels stepped alone, across a
+    join at an odd step, graph-captured chunks, an odd remainder and leaving again."""
+    from luxum_gb300 import Batch
+
+    kw = dict(isPlanar=1, Nx=1500, Ny=1, Nz=1460, **cases.pw((1, 0, 0), (0, 1, 0), ((30, 1469), (0, 0), (30, 1429))),
+              **cases.pml(16), precision=precision)
+    p = cases.make(**kw)
+    boxes = [((600, 0, 500), (800, 1, 900), 3.0)]
+    a, b = _pair(p, boxes)
+    small, small_b = _pair(*_small("planar_pml_axis", precision))
+    for s in (a, b):
+        s.step(7)  # joins at an odd step
+    batch = Batch(chunk=10)
+    batch.add(a)
+    batch.add(small)
+    batch.step(43)  # four captured chunks and an odd remainder
+    batch.step(20)
+    b.step(63)
+    small_b.step(63)
+    _same(a, b)
+    _same(small, small_b)
+    batch.remove(a)
+    a.step(5)
+    b.step(5)
+    _same(a, b)
+    assert a.max_e2() > 0
