@@ -74,11 +74,12 @@ def planar_params(precision: int, n: int):
                   sigma_m=3.0, kappa=5.0, a_max=0.05, a_m=1.0, precision=precision, n_threads=1, monitor_every=1)
 
 
-def profile_case(n: int, steps: int, precision: int, planar: bool = False) -> None:
+def profile_case(n: int, steps: int, precision: int, planar: bool = False, io: bool = False) -> None:
     """Small case for ncu captures: the workload at n^3 (n=192: 0.6 GB resident at FP64,
     above the 129 MB L2), `steps` time steps after 60 untimed ones (wave inside the box).
     planar: the 512^2 layout at n^2 with its centred eps_r 10.89 square (n=4096: 0.47 GB at
-    FP32 with the second state buffer)."""
+    FP32 with the second state buffer).  io (3-D): the 8 probes every step and Ex..Hz
+    snapshots every 2 steps, as the drop-in workload records them (probe and gather kernels)."""
     import __graft_entry__
 
     __graft_entry__.build()
@@ -99,6 +100,9 @@ def profile_case(n: int, steps: int, precision: int, planar: bool = False) -> No
     sim = Sim(workload_params(precision, n))
     a, b = n * 104 // 256, n * 152 // 256
     sim.set_eps_box((a, a, a), (b, b, b), 6.0)
+    if io:
+        sim.set_probes(np.clip(probe_points() * n // N, 1, n - 2), 60 + steps)
+        sim.set_snapshots(2, 0x3F, lambda t, c, arr: None)
     sim.step(60)
     sim.step(steps)
     sim.sync()
@@ -415,16 +419,17 @@ def lens_sims(n_sims: int, seed: int, precision: int, steps: int):
     return sims
 
 
-def box_sims(n_sims: int, seed: int, precision: int, steps: int):
+def box_sims(n_sims: int, seed: int, precision: int, steps: int, side=(64, 192)):
     """3-D batch workload: cubes of side U{64..192} (seeded), the serving requests' 3-D form:
     textbook CPML of min(16, side/8) cells, an Ez plane wave along x through a TF/SF box as
-    deep again, and 1-4 dielectric boxes with eps_r ~ U(1, 12)."""
+    deep again, and 1-4 dielectric boxes with eps_r ~ U(1, 12).  `side`: another side range
+    (cubes under 64^3 share the batched 3-D launches; larger ones are launched one by one)."""
     from luxum_gb300 import Sim
 
     rng = np.random.default_rng(seed)
     sims = []
     for q in range(n_sims):
-        n = int(rng.integers(64, 193))
+        n = int(rng.integers(side[0], side[1] + 1))
         m = serve_margin(n)
         p = serve_params({"side": n, "planar": False})
         p.precision = precision
@@ -441,13 +446,13 @@ def box_sims(n_sims: int, seed: int, precision: int, steps: int):
 
 
 def run_batch(n_sims: int, steps: int, three: bool, runs: int, solo_sample: int, solo_steps: int, peak: float,
-              peak_kind: str) -> dict:
+              peak_kind: str, side=(64, 192)) -> dict:
     """Uneven simulations stepped as one batch: planar lenses, or 3-D cubes (three)."""
     import torch
 
     from luxum_gb300 import Batch, step_bytes
 
-    sims = box_sims(n_sims, 6, 1, steps) if three else lens_sims(n_sims, 4, 1, steps)
+    sims = box_sims(n_sims, 6, 1, steps, side) if three else lens_sims(n_sims, 4, 1, steps)
     cells = sum(s.p.Nx * s.p.Ny * s.p.Nz for s in sims)
     bytes_step = sum(step_bytes(s.p) for s in sims)
     batch = Batch(chunk=100)
@@ -484,7 +489,7 @@ def run_batch(n_sims: int, steps: int, three: bool, runs: int, solo_sample: int,
         s.step(solo_steps)
         s.sync()
     solo = scells * solo_steps / (time.perf_counter() - t0) / 1e9
-    desc = (f"batch of {len(sims)} 3-D simulations, cubes of side U{{64..192}} seed 6, CPML min(16, side/8), TF/SF "
+    desc = (f"batch of {len(sims)} 3-D simulations, cubes of side U{{{side[0]}..{side[1]}}} seed 6, CPML min(16, side/8), TF/SF "
             f"plane wave, 1-4 eps boxes, FP32, {steps} steps, graph chunks of 100" if three else
             f"batch of {len(sims)} planar lens simulations, sides U{{128..1024}} seed 4, "
             f"CPML 16, TF/SF normal incidence, FP32, {steps} steps, graph chunks of 100")
@@ -510,7 +515,8 @@ def bench_batch(args):
     __graft_entry__.build()
     peak, kind = measured_peaks()
     print(json.dumps(run_batch(args.batch_sims, args.batch_steps, args.config == "batch3d", args.steps,
-                               args.solo_sample, args.solo_steps, peak, kind)), flush=True)
+                               args.solo_sample, args.solo_steps, peak, kind,
+                               (args.batch_side_lo, args.batch_side_hi))), flush=True)
 
 
 def serve_requests(n: int, seed: int, rate: float):
@@ -865,6 +871,9 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--precision", type=int, default=0, help="profiling case precision: 0 fp64, 1 fp32, 2 fp16")
     ap.add_argument("--planar", action="store_true", help="profiling case: the planar layout at N^2")
+    ap.add_argument("--profile-io", action="store_true", help="profiling case (3-D): probes and snapshots too")
+    ap.add_argument("--batch-side-lo", type=int, default=64, help="batch3d: smallest cube side")
+    ap.add_argument("--batch-side-hi", type=int, default=192, help="batch3d: largest cube side")
     ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "batch3d", "serve", "phc"],
                     help="drop-in: the headline 256^3 FP64 workload; batch: 256 uneven planar simulations")
     ap.add_argument("--batch-sims", type=int, default=256)
@@ -885,7 +894,7 @@ def main():
     if args.config == "phc":
         return bench_phc(args)
     if args.profile:
-        return profile_case(args.profile, args.profile_steps, args.precision, args.planar)
+        return profile_case(args.profile, args.profile_steps, args.precision, args.planar, args.profile_io)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -904,72 +904,73 @@ __global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __rest
 
 // ------------------------------------------------------------------ data movement
 
-// padded (Nx,Ny,Nzp) storage -> dense double array of extent (n0,n1,n2)
+// The three kernels below walk an (n0, n1, n2) block of a padded (Nx, Ny, Nzp) array one
+// warp per (i, j) row: the row index fits 32 bits (the launchers hold n0*n1 to 2^30), one division
+// per row gives (i, j), and the lanes stride the row's k.  An element-wise 64-bit q -> (i, j, k)
+// split costs two 64-bit divisions per element, which the GPU emulates on the FP64 pipe.
+constexpr int kRowWarps = 8;  // warps (rows in flight) per 256-thread block
+
+__device__ __forceinline__ double as_double(double v) { return v; }
+__device__ __forceinline__ double as_double(float v) { return (double)v; }
+__device__ __forceinline__ double as_double(__half v) { return (double)__half2float(v); }
+
+// padded storage -> dense double array of extent (n0,n1,n2)
 template <class T>
-__global__ void gather_kernel(const T* __restrict__ src, double* __restrict__ dst, int n0, int n1, int n2, int Ny,
-                              int Nzp, double mul) {
-  const long long total = (long long)n0 * n1 * n2;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(q % n2);
-    const long long r = q / n2;
-    const int j = (int)(r % n1);
-    const int i = (int)(r / n1);
-    const double v = (double)src[((long long)i * Ny + j) * Nzp + k];
-    dst[q] = mul == 1.0 ? v : v * mul;
-  }
-}
-template <>
-__global__ void gather_kernel<__half>(const __half* __restrict__ src, double* __restrict__ dst, int n0, int n1, int n2,
-                                      int Ny, int Nzp, double mul) {
-  const long long total = (long long)n0 * n1 * n2;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(q % n2);
-    const long long r = q / n2;
-    const int j = (int)(r % n1);
-    const int i = (int)(r / n1);
-    dst[q] = (double)__half2float(src[((long long)i * Ny + j) * Nzp + k]) * mul;
+__global__ void __launch_bounds__(256) gather_kernel(const T* __restrict__ src, double* __restrict__ dst, int n0,
+                                                     int n1, int n2, int Ny, int Nzp, double mul) {
+  const int lane = threadIdx.x & 31;
+  const int rows = n0 * n1;
+  for (int r = blockIdx.x * kRowWarps + (threadIdx.x >> 5); r < rows; r += gridDim.x * kRowWarps) {
+    const int i = r / n1, j = r - i * n1;
+    const T* s = src + ((long long)i * Ny + j) * Nzp;
+    double* d = dst + (long long)r * n2;
+    for (int k = lane; k < n2; k += 32) {
+      const double v = as_double(s[k]);
+      d[k] = mul == 1.0 ? v : v * mul;
+    }
   }
 }
 
 // dense double array -> padded storage (optionally Cb-style transform)
 // mode 0: dst = v; mode 1: dst = v * a (Cb -> Cb/dx); mode 2: Cb = dt/(eps0*(1+F*scale)) * a
 template <class T>
-__global__ void scatter_kernel(const double* __restrict__ src, T* __restrict__ dst, int n0, int n1, int n2, int Ny,
-                               int Nzp, int mode, double a, double dt, double eps0, double scale) {
-  const long long total = (long long)n0 * n1 * n2;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(q % n2);
-    const long long r = q / n2;
-    const int j = (int)(r % n1);
-    const int i = (int)(r / n1);
-    double v = src[q];
-    if (mode == 2) {
-      // epsilon0*(1+F*1000000) then dt/that (three_dim_pml.cc:122-128), no contraction
-      const double e = __dmul_rn(eps0, __dadd_rn(1.0, __dmul_rn(v, scale)));
-      v = __ddiv_rn(dt, e);
+__global__ void __launch_bounds__(256) scatter_kernel(const double* __restrict__ src, T* __restrict__ dst, int n0,
+                                                      int n1, int n2, int Ny, int Nzp, int mode, double a, double dt,
+                                                      double eps0, double scale) {
+  const int lane = threadIdx.x & 31;
+  const int rows = n0 * n1;
+  for (int r = blockIdx.x * kRowWarps + (threadIdx.x >> 5); r < rows; r += gridDim.x * kRowWarps) {
+    const int i = r / n1, j = r - i * n1;
+    const double* s = src + (long long)r * n2;
+    T* d = dst + ((long long)i * Ny + j) * Nzp;
+    for (int k = lane; k < n2; k += 32) {
+      double v = s[k];
+      if (mode == 2) {
+        // epsilon0*(1+F*1000000) then dt/that (three_dim_pml.cc:122-128), no contraction
+        const double e = __dmul_rn(eps0, __dadd_rn(1.0, __dmul_rn(v, scale)));
+        v = __ddiv_rn(dt, e);
+      }
+      if (mode >= 1) v = __dmul_rn(v, a);
+      if constexpr (sizeof(T) == 2) d[k] = __double2half(v);
+      else d[k] = (T)v;
     }
-    if (mode >= 1) v = __dmul_rn(v, a);
-    const long long o = ((long long)i * Ny + j) * Nzp + k;
-    if constexpr (sizeof(T) == 2) dst[o] = __double2half(v);
-    else dst[o] = (T)v;
   }
 }
 
 // Cb = dt/(eps0*eps_r) * a over the box [lo, hi) clipped to the extent
 template <class C>
-__global__ void eps_box_kernel(C* dst, int n0, int n1, int n2, int Ny, int Nzp, int lo0, int lo1, int lo2, int hi0,
-                               int hi1, int hi2, double val) {
+__global__ void __launch_bounds__(256) eps_box_kernel(C* dst, int n0, int n1, int n2, int Ny, int Nzp, int lo0,
+                                                      int lo1, int lo2, int hi0, int hi1, int hi2, double val) {
   const int a0 = max(lo0, 0), a1 = max(lo1, 0), a2 = max(lo2, 0);
   const int b0 = min(hi0, n0), b1 = min(hi1, n1), b2 = min(hi2, n2);
   if (a0 >= b0 || a1 >= b1 || a2 >= b2) return;
-  const long long w0 = b0 - a0, w1 = b1 - a1, w2 = b2 - a2;
-  const long long total = w0 * w1 * w2;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
-    const int k = a2 + (int)(q % w2);
-    const long long r = q / w2;
-    const int j = a1 + (int)(r % w1);
-    const int i = a0 + (int)(r / w1);
-    dst[((long long)i * Ny + j) * Nzp + k] = (C)val;
+  const int w1 = b1 - a1;
+  const int rows = (b0 - a0) * w1;
+  const int lane = threadIdx.x & 31;
+  for (int r = blockIdx.x * kRowWarps + (threadIdx.x >> 5); r < rows; r += gridDim.x * kRowWarps) {
+    const int di = r / w1;
+    C* d = dst + ((long long)(a0 + di) * Ny + a1 + (r - di * w1)) * Nzp;
+    for (int k = a2 + lane; k < b2; k += 32) d[k] = (C)val;
   }
 }
 
@@ -1123,6 +1124,12 @@ __global__ void dft_flux_final(const double* __restrict__ part, int nfreq, int n
 
 // ------------------------------------------------------------------ launchers
 
+// Blocks for a row-walking kernel: one warp per row, at most 16 blocks of 8 warps per SM.
+static inline unsigned row_grid(long long rows) {
+  const long long b = (rows + kRowWarps - 1) / kRowWarps;
+  return (unsigned)(b < 152 * 16 ? b : 152 * 16);
+}
+
 static inline unsigned grid1d(long long n, int bs) {
   long long g = (n + bs - 1) / bs;
   if (g > 152LL * 64) g = 152LL * 64;
@@ -1196,24 +1203,27 @@ cudaError_t launch_step_sweep2(const StepParams<T, C>& p, bool uniform, cudaStre
 
 template <class T>
 cudaError_t launch_gather(const T* src, double* dst, const int ext[3], int Ny, int Nzp, double mul, cudaStream_t s) {
-  const long long n = (long long)ext[0] * ext[1] * ext[2];
-  if (n == 0) return cudaSuccess;
-  gather_kernel<T><<<grid1d(n, 256), 256, 0, s>>>(src, dst, ext[0], ext[1], ext[2], Ny, Nzp, mul);
+  const long long rows = (long long)ext[0] * ext[1];
+  if (rows == 0 || ext[2] == 0) return cudaSuccess;
+  if (rows > (1LL << 30)) return cudaErrorInvalidValue;  // r + stride stays in int
+  gather_kernel<T><<<row_grid(rows), 256, 0, s>>>(src, dst, ext[0], ext[1], ext[2], Ny, Nzp, mul);
   return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t launch_scatter(const double* src, T* dst, const int ext[3], int Ny, int Nzp, int mode, double a, double dt,
                            double eps0, double scale, cudaStream_t s) {
-  const long long n = (long long)ext[0] * ext[1] * ext[2];
-  if (n == 0) return cudaSuccess;
-  scatter_kernel<T><<<grid1d(n, 256), 256, 0, s>>>(src, dst, ext[0], ext[1], ext[2], Ny, Nzp, mode, a, dt, eps0, scale);
+  const long long rows = (long long)ext[0] * ext[1];
+  if (rows == 0 || ext[2] == 0) return cudaSuccess;
+  if (rows > (1LL << 30)) return cudaErrorInvalidValue;  // r + stride stays in int
+  scatter_kernel<T><<<row_grid(rows), 256, 0, s>>>(src, dst, ext[0], ext[1], ext[2], Ny, Nzp, mode, a, dt, eps0, scale);
   return cudaGetLastError();
 }
 
 template <class C>
 cudaError_t launch_eps_box(C* dst, const int ext[3], int Ny, int Nzp, const int lo[3], const int hi[3], double val,
                            cudaStream_t s) {
+  if ((long long)ext[0] * ext[1] > (1LL << 30)) return cudaErrorInvalidValue;
   eps_box_kernel<C><<<152 * 4, 256, 0, s>>>(dst, ext[0], ext[1], ext[2], Ny, Nzp, lo[0], lo[1], lo[2], hi[0], hi[1],
                                             hi[2], val);
   return cudaGetLastError();
