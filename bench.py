@@ -493,6 +493,7 @@ def run_batch(n_sims: int, steps: int, three: bool, runs: int, solo_sample: int,
             f"plane wave, 1-4 eps boxes, FP32, {steps} steps, graph chunks of 100" if three else
             f"batch of {len(sims)} planar lens simulations, sides U{{128..1024}} seed 4, "
             f"CPML 16, TF/SF normal incidence, FP32, {steps} steps, graph chunks of 100")
+    table = batch.tune_table()
     batch.close()
     for s in sims:
         s.close()
@@ -504,7 +505,7 @@ def run_batch(n_sims: int, steps: int, three: bool, runs: int, solo_sample: int,
             "unbatched_sample": {"sims": len(sample), "value": solo, "steps": solo_steps,
                                  "note": "same simulations stepped one handle at a time with lx_sim_step"},
             "batched_over_unbatched": value / solo, "autotuned_march": {"planar_rows": march[0], "planes_3d": march[1],
-                                                                       "seconds": t_tune},
+                                                                       "table": table, "seconds": t_tune},
             "clocks": clk.summary()}
 
 
@@ -600,6 +601,7 @@ def run_serve(n_requests: int, rate: float, budget_gb: float, chunk: int, peak: 
             srv.release(rid)
         wall = time.perf_counter() - t0
     st = srv.stats()
+    table = srv.tune_table()
     srv.close()
     lat = np.array(lat)
     offered = sum(r["side"] ** (2 if r["planar"] else 3) for r in reqs) * SERVE_STEPS / reqs[-1]["arrival"] / 1e9
@@ -614,7 +616,11 @@ def run_serve(n_requests: int, rate: float, budget_gb: float, chunk: int, peak: 
                                  note="compulsory bytes of every completed request over the stream's wall time"),
             "sustained": bool(work / wall / 1e9 >= 0.95 * offered),
             "peak_running": st["peak_running"], "peak_budget_gb": st["peak_bytes_running"] / 1e9,
-            "chunks": st["chunks"], "gpu_busy_s": st["busy_seconds"], "dtype": "f32", "clocks": clk.summary()}
+            "chunks": st["chunks"], "gpu_busy_s": st["busy_seconds"],
+            "tuned_march": {"table": table, "seconds": st["tune_seconds"],
+                            "note": "tile shape per request class, tuned on twins of its first request before it "
+                                    "joined (inside the stream's wall time)"},
+            "dtype": "f32", "clocks": clk.summary()}
 
 
 def bench_serve(args):

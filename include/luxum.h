@@ -287,10 +287,33 @@ LX_API lx_status lx_batch_wait(lx_batch* b);
  * (defaults 8, 8).  Results do not depend on it, only speed. */
 LX_API lx_status lx_batch_set_march(lx_batch* b, int planar_rows, int planes_3d);
 LX_API lx_status lx_batch_get_march(const lx_batch* b, int* planar_rows, int* planes_3d);
-/* Picks the march per dimension by timing `steps` batched steps of each candidate on
- * zero-field twins of a sample of the members (up to 1.5e8 cells per dimension, created
- * and freed here); the members themselves are not stepped.  Reports the choice. */
+/* Tile-shape table.  Members are classed by (dimension, size, precision, CPML slab depth);
+ * a class with an entry takes that entry's march, the others the per-dimension march above.
+ * Members of different classes whose marches differ take separate launches. */
+typedef struct lx_tune_entry {
+  int planar;      /* 1 planar, 0 3-D */
+  int size_class;  /* floor(log4(Nx*Ny*Nz)), at most 15 */
+  int precision;   /* LX_PREC_* */
+  int slab_class;  /* CPML slab depth along x: 0 none, 1 up to 8 cells, 2 up to 16, 3 deeper */
+  int march;       /* 1, 2, 4 or 8 */
+} lx_tune_entry;
+/* Fills every field of *key but march with the handle's class. */
+LX_API lx_status lx_sim_tune_class(const lx_sim* sim, lx_tune_entry* key);
+/* Replaces the batch's table (n entries; n = 0 clears it).  Duplicate classes: the last wins. */
+LX_API lx_status lx_batch_set_tune_table(lx_batch* b, const lx_tune_entry* entries, int n);
+/* Copies up to cap entries to entries (may be NULL when cap is 0); *n = the table's length. */
+LX_API lx_status lx_batch_get_tune_table(const lx_batch* b, lx_tune_entry* entries, int cap, int* n);
+/* Tunes the class of every batched member (3-D members of 2^18 cells or more and planar
+ * single-sweep members are launched one by one and have no tile shape): for each class, times
+ * `steps` batched steps of each march on zero-field twins of a sample of the class's members
+ * (up to 1.5e8 cells, created and freed here) and records the fastest in the table.  The
+ * members themselves are not stepped.  The per-dimension march becomes the pick of the
+ * dimension's largest class (by cells) and is reported. */
 LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* planar_rows, int* planes_3d);
+/* Tunes the class of one handle (not necessarily a member yet) on zero-field twins of it,
+ * replicated up to 2^22 cells or 16 twins, and records the pick; *march = 0 when the class has
+ * no tile shape.  The handle is not stepped.  Waits for the batch's enqueued steps. */
+LX_API lx_status lx_batch_tune_member(lx_batch* b, const lx_sim* sim, int steps, int* march);
 
 /* ---- Serving: continuous batching of submitted simulations --------------------------
  * No reference counterpart: the reference runs one simulation per process.  A server owns
@@ -306,6 +329,9 @@ typedef struct lx_server_config {
   int chunk;              /* steps per batch launch, captured as a CUDA graph (default 100) */
   double budget_bytes;    /* device memory for running requests (default 0: 90% of free) */
   int max_running;        /* 0: no limit besides the budget */
+  int tune_steps;         /* > 0: tune each new class of batched request on twins of it before
+                             it joins (lx_batch_tune_member, `tune_steps` steps per march);
+                             0: the default tile shapes (default 10) */
 } lx_server_config;
 LX_API void lx_server_config_init(lx_server_config* cfg);
 
@@ -336,6 +362,8 @@ typedef struct lx_server_stats {
   double cell_updates;        /* over all chunks stepped */
   double busy_seconds;        /* worker time with requests running */
   long long chunks;
+  double tune_seconds;        /* worker time spent tuning classes (outside busy_seconds) */
+  int tuned_classes;
 } lx_server_stats;
 
 LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_server** out);
@@ -365,6 +393,8 @@ LX_API lx_status lx_server_release(lx_server* srv, long long id);
 /* Why a request FAILED ("" otherwise); valid until the request is released. */
 LX_API const char* lx_server_error(lx_server* srv, long long id);
 LX_API lx_status lx_server_stats_get(lx_server* srv, lx_server_stats* st);
+/* The server batch's tile-shape table (lx_batch_get_tune_table). */
+LX_API lx_status lx_server_tune_table(lx_server* srv, lx_tune_entry* entries, int cap, int* n);
 
 /* A batch is driven by one host thread at a time (the server's worker drives its own). */
 

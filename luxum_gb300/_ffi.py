@@ -62,7 +62,13 @@ class Info(C.Structure):
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("precision", C.c_int), ("chunk", C.c_int), ("budget_bytes", C.c_double), ("max_running", C.c_int)]
+    _fields_ = [("precision", C.c_int), ("chunk", C.c_int), ("budget_bytes", C.c_double), ("max_running", C.c_int),
+                ("tune_steps", C.c_int)]
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("planar", C.c_int), ("size_class", C.c_int), ("precision", C.c_int), ("slab_class", C.c_int),
+                ("march", C.c_int)]
 
 
 class Request(C.Structure):
@@ -76,7 +82,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("queued", C.c_longlong), ("running", C.c_longlong),
                 ("done", C.c_longlong), ("failed", C.c_longlong), ("cancelled", C.c_longlong),
                 ("bytes_running", C.c_double), ("peak_bytes_running", C.c_double), ("peak_running", C.c_int),
-                ("cell_updates", C.c_double), ("busy_seconds", C.c_double), ("chunks", C.c_longlong)]
+                ("cell_updates", C.c_double), ("busy_seconds", C.c_double), ("chunks", C.c_longlong),
+                ("tune_seconds", C.c_double), ("tuned_classes", C.c_int)]
 
 
 SNAPSHOT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int))
@@ -141,6 +148,10 @@ def declare(lib) -> None:
     _proto(lib, "lx_batch_set_march", C.c_int, C.c_void_p, C.c_int, C.c_int)
     _proto(lib, "lx_batch_get_march", C.c_int, C.c_void_p, P(C.c_int), P(C.c_int))
     _proto(lib, "lx_batch_autotune", C.c_int, C.c_void_p, C.c_int, P(C.c_int), P(C.c_int))
+    _proto(lib, "lx_sim_tune_class", C.c_int, C.c_void_p, P(TuneEntry))
+    _proto(lib, "lx_batch_set_tune_table", C.c_int, C.c_void_p, P(TuneEntry), C.c_int)
+    _proto(lib, "lx_batch_get_tune_table", C.c_int, C.c_void_p, P(TuneEntry), C.c_int, P(C.c_int))
+    _proto(lib, "lx_batch_tune_member", C.c_int, C.c_void_p, C.c_void_p, C.c_int, P(C.c_int))
     srv, ll = C.c_void_p, C.c_longlong
     _proto(lib, "lx_params_field_shape", C.c_int, P(Params), C.c_int, P(C.c_int))
     _proto(lib, "lx_server_config_init", None, P(ServerConfig))
@@ -158,6 +169,7 @@ def declare(lib) -> None:
     _proto(lib, "lx_server_release", C.c_int, srv, ll)
     _proto(lib, "lx_server_error", C.c_char_p, srv, ll)
     _proto(lib, "lx_server_stats_get", C.c_int, srv, P(ServerStats))
+    _proto(lib, "lx_server_tune_table", C.c_int, srv, P(TuneEntry), C.c_int, P(C.c_int))
     _proto(lib, "lx_host_alloc", C.c_int, C.c_size_t, P(C.c_void_p))
     _proto(lib, "lx_host_free", None, C.c_void_p)
     _proto(lib, "lx_last_error", C.c_char_p, sim)

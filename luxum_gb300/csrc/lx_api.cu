@@ -1800,6 +1800,7 @@ struct lx_batch {
     int nblocks = 0;
   };
   int march2d = lx::kMarch2, march3d = lx::kMarch3;  // per dimension (lx_batch_set_march / autotune)
+  std::vector<lx_tune_entry> table;  // march per member class (lx_batch_set_tune_table / autotune)
   struct DftClass {  // DFT planes that sample at the same batch steps
     int every = 1, phase = 0;
     lx::DftParams* d_planes = nullptr;
@@ -1824,6 +1825,49 @@ struct lx_batch {
 };
 
 static void batch_member_changed(lx_batch* b) { b->dirty = true; }
+
+// A member launched one by one, with no tile shape: 3-D members of kSoloCells cells or more,
+// planar single-sweep members of kSoloCells2 cells or more.
+static bool batch_alone(const lx_sim* s) {
+  return s->planar ? s->sweep && (long long)s->Nx * s->Nz >= lx_batch::kSoloCells2
+                   : (long long)s->Nx * s->Ny * s->Nz >= lx_batch::kSoloCells;
+}
+
+// The tile-shape class of a handle: dimension, floor(log4(cells)), precision, x slab depth.
+static lx_tune_entry tune_class_of(const lx_sim* s) {
+  lx_tune_entry e{};
+  const double cells = (double)s->Nx * s->Ny * s->Nz;
+  int sc = 0;
+  while (sc < 15 && cells >= std::ldexp(1.0, 2 * (sc + 1))) sc++;
+  e.planar = s->planar ? 1 : 0;
+  e.size_class = sc;
+  e.precision = s->p.precision;
+  const int d = s->pml ? s->slab[0].lo : 0;
+  e.slab_class = d <= 0 ? 0 : d <= 8 ? 1 : d <= 16 ? 2 : 3;
+  return e;
+}
+
+static bool same_class(const lx_tune_entry& a, const lx_tune_entry& b) {
+  return a.planar == b.planar && a.size_class == b.size_class && a.precision == b.precision &&
+         a.slab_class == b.slab_class;
+}
+
+static void table_put(lx_batch* b, const lx_tune_entry& e) {
+  for (auto& x : b->table)
+    if (same_class(x, e)) {
+      x.march = e.march;
+      return;
+    }
+  b->table.push_back(e);
+}
+
+// The march of a batched member: its class's table entry, else the per-dimension march.
+static int batch_march(const lx_batch* b, const lx_sim* s) {
+  const lx_tune_entry k = tune_class_of(s);
+  for (const auto& x : b->table)
+    if (same_class(x, k)) return x.march;
+  return s->planar ? b->march2d : b->march3d;
+}
 
 static void batch_free_device(lx_batch* b) {
   for (auto& g : b->groups) {
@@ -1960,7 +2004,7 @@ static lx_status batch_rebuild(lx_batch* b) {
   // a member whose mode changes at an odd step moves its state (one device copy).
   for (int q = 0; q < n; q++) {
     lx_sim* s = b->sims[q];
-    const bool two = s->sweep && s->planar && (long long)s->Nx * s->Nz >= lx_batch::kSoloCells2;
+    const bool two = s->planar && batch_alone(s);
     lx_status st;
     if ((st = set_pp(s, two))) return st;
     BCK(cudaStreamSynchronize(s->stream));
@@ -1999,19 +2043,21 @@ static lx_status batch_rebuild(lx_batch* b) {
       dft_planes[ci].push_back(dp);
       if (b->chunk > 0 && b->chunk % d.every != 0) b->graphable = false;
     }
-    const bool solo = s->pp || (!s->planar && (long long)s->Nx * s->Ny * s->Nz >= lx_batch::kSoloCells);
+    const bool solo = s->pp || (!s->planar && batch_alone(s));
     if (s->pp && b->chunk % 2) b->graphable = false;  // a captured chunk must keep each member's parity
+    // batched members share a launch only with members of the same march (their classes' picks)
+    const int march = solo ? (s->planar ? b->march2d : b->march3d) : batch_march(b, s);
     int gi = -1;
     for (size_t g = 0; g < b->groups.size(); g++)
       if (b->groups[g].planar == (bool)s->planar && b->groups[g].uniform == (bool)s->uniform &&
-          b->groups[g].solo == solo)
+          b->groups[g].solo == solo && (solo || b->groups[g].march == march))
         gi = (int)g;
     if (gi < 0) {
       b->groups.emplace_back();
       b->groups.back().planar = s->planar;
       b->groups.back().uniform = s->uniform;
       b->groups.back().solo = solo;
-      b->groups.back().march = s->planar ? b->march2d : b->march3d;
+      b->groups.back().march = march;
       gi = (int)b->groups.size() - 1;
     }
     b->groups[gi].members.push_back(q);
@@ -2216,34 +2262,24 @@ extern "C" LX_API lx_status lx_batch_get_march(const lx_batch* b, int* planar_ro
   return LX_OK;
 }
 
-// Times `steps` batched steps of twins (zero fields, same parameters and Cb) of a sample of
-// the members of one dimension for each march length, on a scratch batch; the members
-// themselves are not touched.  Returns the fastest march, or 0 if there is nothing to time.
-static lx_status tune_dimension(lx_batch* b, bool planar, int steps, double cell_budget, int* best) {
+// Times `steps` batched steps of twins (zero fields, same parameters and Cb) of `sample`, each
+// member `copies` times, on a scratch batch for each march length; the sampled handles
+// themselves are not touched.  *best = the fastest march.
+static lx_status time_marches(const std::vector<const lx_sim*>& sample, int copies, int steps, int* best) {
   *best = 0;
-  std::vector<lx_sim*> sample;
-  double cells = 0.0;
-  for (auto* s : b->sims) {
-    if ((bool)s->planar != planar) continue;
-    const double c = (double)s->Nx * s->Ny * s->Nz;
-    if (!planar && c >= (double)lx_batch::kSoloCells) continue;  // launched one by one: no tile shape
-    if (!sample.empty() && cells + c > cell_budget) continue;
-    sample.push_back(s);
-    cells += c;
-  }
-  if (sample.empty()) return LX_OK;
   std::vector<lx_sim*> twins;
   lx_batch* tb = nullptr;
   lx_status st = lx_batch_create(&tb);
   if (!st) st = lx_batch_set_chunk(tb, 0);
-  for (size_t q = 0; q < sample.size() && !st; q++) {
+  for (size_t q = 0; q < sample.size() * copies && !st; q++) {
+    const lx_sim* src = sample[q % sample.size()];
     lx_sim* t = nullptr;
-    st = lx_sim_create(&sample[q]->p, &t);
+    st = lx_sim_create(&src->p, &t);
     if (st) break;
     twins.push_back(t);
     for (int c = 0; c < 3 && !st; c++)
-      if (sample[q]->Cbs[c] && ext_n(sample[q], c))
-        if (cudaMemcpyAsync(t->Cbs[c], sample[q]->Cbs[c], t->ncell * t->csize, cudaMemcpyDeviceToDevice, t->stream) != cudaSuccess)
+      if (src->Cbs[c] && ext_n(src, c))
+        if (cudaMemcpyAsync(t->Cbs[c], src->Cbs[c], t->ncell * t->csize, cudaMemcpyDeviceToDevice, t->stream) != cudaSuccess)
           st = fail(nullptr, LX_ERR_CUDA, "copying Cb to a tuning twin failed");
     if (!st) st = lx_sim_sync(t);
     if (!st) st = lx_batch_add(tb, t);
@@ -2276,17 +2312,110 @@ static lx_status tune_dimension(lx_batch* b, bool planar, int steps, double cell
   return st;
 }
 
+// Drops the captured graph and regroups the members at the next step (a march changed).
+static void batch_reshape(lx_batch* b) {
+  b->dirty = true;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  b->exec_steps = 0;
+}
+
+extern "C" LX_API lx_status lx_sim_tune_class(const lx_sim* s, lx_tune_entry* key) {
+  if (!s || !key) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  *key = tune_class_of(s);
+  key->march = 0;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_batch_set_tune_table(lx_batch* b, const lx_tune_entry* e, int n) {
+  if (!b || n < 0 || (n > 0 && !e)) return fail(nullptr, LX_ERR_INVALID, "bad table");
+  for (int q = 0; q < n; q++)
+    if (!march_ok(e[q].march) || e[q].planar < 0 || e[q].planar > 1 || e[q].size_class < 0 || e[q].size_class > 15 ||
+        e[q].precision < LX_PREC_FP64 || e[q].precision > LX_PREC_FP16S || e[q].slab_class < 0 || e[q].slab_class > 3)
+      return fail(nullptr, LX_ERR_INVALID, "bad table entry (march 1, 2, 4 or 8; classes as lx_sim_tune_class)");
+  lx::DeviceGuard dg_(b->device);
+  lx_status st = lx_batch_wait(b);
+  if (st) return st;
+  b->table.clear();
+  for (int q = 0; q < n; q++) table_put(b, e[q]);
+  batch_reshape(b);
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_batch_get_tune_table(const lx_batch* b, lx_tune_entry* e, int cap, int* n) {
+  if (!b || !n || cap < 0 || (cap > 0 && !e)) return fail(nullptr, LX_ERR_INVALID, "null argument");
+  for (int q = 0; q < cap && q < (int)b->table.size(); q++) e[q] = b->table[q];
+  *n = (int)b->table.size();
+  return LX_OK;
+}
+
 extern "C" LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* planar_rows, int* planes_3d) {
   if (!b || steps < 1) return fail(nullptr, LX_ERR_INVALID, "steps must be >= 1");
   lx::DeviceGuard dg_(b->device);
   lx_status st = lx_batch_wait(b);
   if (st) return st;
+  // the classes of the batched members, with a sample of each up to the cell budget
+  const double budget = 1.5e8;
+  std::vector<lx_tune_entry> classes;
+  std::vector<std::vector<const lx_sim*>> samples;
+  std::vector<double> sampled, total;
+  for (auto* s : b->sims) {
+    if (batch_alone(s)) continue;
+    const lx_tune_entry k = tune_class_of(s);
+    size_t c = 0;
+    while (c < classes.size() && !same_class(classes[c], k)) c++;
+    if (c == classes.size()) {
+      classes.push_back(k);
+      samples.emplace_back();
+      sampled.push_back(0.0);
+      total.push_back(0.0);
+    }
+    const double cells = (double)s->Nx * s->Ny * s->Nz;
+    total[c] += cells;
+    if (samples[c].empty() || sampled[c] + cells <= budget) {
+      samples[c].push_back(s);
+      sampled[c] += cells;
+    }
+  }
   int m2 = 0, m3 = 0;
-  const double budget = 1.5e8;  // cells of twins per dimension
-  if ((st = tune_dimension(b, true, steps, budget, &m2))) return st;
-  if ((st = tune_dimension(b, false, steps, budget, &m3))) return st;
+  double big2 = -1.0, big3 = -1.0;
+  for (size_t c = 0; c < classes.size(); c++) {
+    int best = 0;
+    if ((st = time_marches(samples[c], 1, steps, &best))) return st;
+    if (!best) continue;
+    classes[c].march = best;
+    table_put(b, classes[c]);
+    double& big = classes[c].planar ? big2 : big3;
+    if (total[c] > big) {
+      big = total[c];
+      (classes[c].planar ? m2 : m3) = best;
+    }
+  }
   if ((st = lx_batch_set_march(b, m2 ? m2 : b->march2d, m3 ? m3 : b->march3d))) return st;
   if (planar_rows) *planar_rows = b->march2d;
   if (planes_3d) *planes_3d = b->march3d;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_batch_tune_member(lx_batch* b, const lx_sim* s, int steps, int* march) {
+  if (!b || !s || steps < 1) return fail(nullptr, LX_ERR_INVALID, "null argument or steps < 1");
+  if (march) *march = 0;
+  if (s->device != b->device) return fail(nullptr, LX_ERR_INVALID, "handle lives on another device than the batch");
+  if (b->prec >= 0 && s->prec != b->prec) return fail(nullptr, LX_ERR_INVALID, "handle precision differs from the batch's");
+  lx::DeviceGuard dg_(b->device);
+  lx_status st = lx_batch_wait(b);
+  if (st) return st;
+  if (batch_alone(s)) return LX_OK;
+  const double cells = (double)s->Nx * s->Ny * s->Nz;
+  const int copies = (int)std::max(1.0, std::min(16.0, std::floor(4194304.0 / std::max(cells, 1.0))));
+  int best = 0;
+  if ((st = time_marches({s}, copies, steps, &best))) return st;
+  if (best) {
+    lx_tune_entry e = tune_class_of(s);
+    e.march = best;
+    table_put(b, e);
+    batch_reshape(b);
+  }
+  if (march) *march = best;
   return LX_OK;
 }

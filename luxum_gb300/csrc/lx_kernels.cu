@@ -920,14 +920,17 @@ __global__ void __launch_bounds__(256) gather_kernel(const T* __restrict__ src, 
                                                      int n1, int n2, int Ny, int Nzp, double mul) {
   const int lane = threadIdx.x & 31;
   const int rows = n0 * n1;
+  const bool scale = mul != 1.0;
   for (int r = blockIdx.x * kRowWarps + (threadIdx.x >> 5); r < rows; r += gridDim.x * kRowWarps) {
     const int i = r / n1, j = r - i * n1;
     const T* s = src + ((long long)i * Ny + j) * Nzp;
     double* d = dst + (long long)r * n2;
-    for (int k = lane; k < n2; k += 32) {
-      const double v = as_double(s[k]);
-      d[k] = mul == 1.0 ? v : v * mul;
-    }
+    // two loops, so that a plain copy issues no FP64 compare or multiply per element (the FP64
+    // pipe is the narrowest on this GPU)
+    if (scale)
+      for (int k = lane; k < n2; k += 32) d[k] = as_double(s[k]) * mul;
+    else
+      for (int k = lane; k < n2; k += 32) d[k] = as_double(s[k]);
   }
 }
 

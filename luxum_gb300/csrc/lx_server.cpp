@@ -21,7 +21,9 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <array>
 #include <map>
+#include <set>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -78,6 +80,8 @@ struct lx_server {
   bool stop = false;
   lx_batch* batch = nullptr;
   lx_server_stats stats;
+  std::set<std::array<int, 4>> tried;    // classes tuned (or found to have no tile shape); worker only
+  std::vector<lx_tune_entry> table;      // copy of the batch's tile-shape table for clients (under mu)
   std::thread worker;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
@@ -194,6 +198,38 @@ void join(lx_server* srv) {
   srv->stats.peak_bytes_running = std::max(srv->stats.peak_bytes_running, srv->stats.bytes_running);
 }
 
+// Tunes the tile shape of each prepared handle's class that has not been tried yet, on twins
+// of the handle (lx_batch_tune_member), before it joins.  Worker only, with the batch idle; the
+// twins are created and freed inside, outside the memory budget.  A failed tuning leaves the
+// default shape.
+void tune_prepared(lx_server* srv) {
+  if (srv->cfg.tune_steps <= 0) return;
+  std::vector<lx_sim*> sims;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (auto& r : srv->prepared)
+      if (!r->cancel && r->sim) sims.push_back(r->sim);
+  }
+  for (lx_sim* s : sims) {
+    lx_tune_entry k;
+    if (lx_sim_tune_class(s, &k)) continue;
+    if (!srv->tried.insert({k.planar, k.size_class, k.precision, k.slab_class}).second) continue;
+    const auto t0 = Clock::now();
+    int m = 0;
+    lx_batch_tune_member(srv->batch, s, srv->cfg.tune_steps, &m);
+    int n = 0;
+    std::vector<lx_tune_entry> table;
+    if (!lx_batch_get_tune_table(srv->batch, nullptr, 0, &n) && n > 0) {
+      table.resize(n);
+      lx_batch_get_tune_table(srv->batch, table.data(), n, &n);
+    }
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->stats.tune_seconds += std::chrono::duration<double>(Clock::now() - t0).count();
+    if (m) srv->stats.tuned_classes += 1;
+    srv->table.swap(table);
+  }
+}
+
 // Retires running requests that finished, blew up or were cancelled (lock held).
 void retire(lx_server* srv) {
   std::vector<std::shared_ptr<Request>> keep;
@@ -228,6 +264,7 @@ void worker_main(lx_server* srv) {
   cudaSetDevice(srv->device);
   for (;;) {
     prepare(srv);
+    tune_prepared(srv);
     int n = 0;
     {
       std::unique_lock<std::mutex> lk(srv->mu);
@@ -299,6 +336,7 @@ extern "C" LX_API void lx_server_config_init(lx_server_config* cfg) {
   std::memset(cfg, 0, sizeof *cfg);
   cfg->precision = LX_PREC_FP32;
   cfg->chunk = 100;
+  cfg->tune_steps = 10;
 }
 
 extern "C" LX_API void lx_request_init(lx_request* r) {
@@ -316,7 +354,7 @@ extern "C" LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_ser
   if (cfg) c = *cfg;
   if (c.precision < LX_PREC_FP64 || c.precision > LX_PREC_FP16S) return sfail(LX_ERR_INVALID, "bad precision");
   if (c.chunk < 1) return sfail(LX_ERR_INVALID, "chunk must be >= 1");
-  if (c.max_running < 0 || c.budget_bytes < 0) return sfail(LX_ERR_INVALID, "negative limit");
+  if (c.max_running < 0 || c.budget_bytes < 0 || c.tune_steps < 0) return sfail(LX_ERR_INVALID, "negative limit");
   if (c.budget_bytes == 0) {
     size_t fr = 0, tot = 0;
     const cudaError_t e = cudaMemGetInfo(&fr, &tot);
@@ -528,5 +566,13 @@ extern "C" LX_API lx_status lx_server_stats_get(lx_server* srv, lx_server_stats*
   if (!srv || !st) return sfail(LX_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(srv->mu);
   *st = srv->stats;
+  return LX_OK;
+}
+
+extern "C" LX_API lx_status lx_server_tune_table(lx_server* srv, lx_tune_entry* e, int cap, int* n) {
+  if (!srv || !n || cap < 0 || (cap > 0 && !e)) return sfail(LX_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  for (int q = 0; q < cap && q < (int)srv->table.size(); q++) e[q] = srv->table[q];
+  *n = (int)srv->table.size();
   return LX_OK;
 }

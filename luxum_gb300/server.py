@@ -20,11 +20,13 @@ STATES = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancelled"}
 
 class Server:
     def __init__(self, precision: int = _ffi.LX_PREC_FP32, chunk: int = 100, budget_bytes: float = 0.0,
-                 max_running: int = 0):
+                 max_running: int = 0, tune_steps: int | None = None):
         self.lib = _ffi.lib()
         cfg = ServerConfig()
         self.lib.lx_server_config_init(C.byref(cfg))
         cfg.precision, cfg.chunk, cfg.budget_bytes, cfg.max_running = precision, chunk, budget_bytes, max_running
+        if tune_steps is not None:
+            cfg.tune_steps = tune_steps
         self.precision = precision
         h = C.c_void_p()
         self._check(self.lib.lx_server_create(C.byref(cfg), C.byref(h)))
@@ -115,6 +117,12 @@ class Server:
         st = ServerStats()
         self._check(self.lib.lx_server_stats_get(self.h, C.byref(st)))
         return {n: getattr(st, n) for n, _ in ServerStats._fields_}
+
+    def tune_table(self) -> list:
+        """The tile shapes the server picked per request class (lx_server_tune_table)."""
+        from .sim import _read_table
+
+        return _read_table(lambda e, cap, n: self.lib.lx_server_tune_table(self.h, e, cap, n), self._check)
 
     def close(self) -> None:
         if getattr(self, "h", None):

@@ -126,6 +126,12 @@ class Sim:
     def t(self) -> int:
         return self.lib.lx_sim_timestep(self.h)
 
+    def tune_class(self) -> dict:
+        """The handle's tile-shape class (planar, size_class, precision, slab_class)."""
+        e = _ffi.TuneEntry()
+        self._check(self.lib.lx_sim_tune_class(self.h, C.byref(e)))
+        return {k: getattr(e, k) for k, _ in _ffi.TuneEntry._fields_ if k != "march"}
+
     def max_e2(self) -> float:
         v = C.c_double()
         self._check(self.lib.lx_sim_max_e2(self.h, C.byref(v)))
@@ -342,10 +348,28 @@ class Batch:
         return a.value, b.value
 
     def autotune(self, steps: int = 20) -> tuple:
-        """Times each march on twins of the members and keeps the fastest; returns (planar, 3-D)."""
+        """Times each march on twins of each class of member and records the fastest per class
+        (tune_table); returns the per-dimension march (planar, 3-D), the largest class's pick."""
         a, b = C.c_int(), C.c_int()
         self._check(self.lib.lx_batch_autotune(self.h, steps, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def tune_member(self, sim, steps: int = 10) -> int:
+        """Tunes the class of `sim` on twins of it; returns the pick (0: no tile shape)."""
+        m = C.c_int()
+        self._check(self.lib.lx_batch_tune_member(self.h, sim.h, steps, C.byref(m)))
+        return m.value
+
+    def tune_table(self) -> list:
+        """The tile-shape table: dicts with planar, size_class, precision, slab_class, march."""
+        return _read_table(lambda e, cap, n: self.lib.lx_batch_get_tune_table(self.h, e, cap, n), self._check)
+
+    def set_tune_table(self, entries) -> None:
+        arr = (_ffi.TuneEntry * max(len(entries), 1))()
+        for q, e in enumerate(entries):
+            for k, _ in _ffi.TuneEntry._fields_:
+                setattr(arr[q], k, int(e[k]))
+        self._check(self.lib.lx_batch_set_tune_table(self.h, arr, len(entries)))
 
     def __len__(self):
         return self.lib.lx_batch_size(self.h)
@@ -360,3 +384,12 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def _read_table(get, check) -> list:
+    """Reads a tile-shape table through get(entries, cap, byref(n))."""
+    n = C.c_int()
+    check(get(None, 0, C.byref(n)))
+    arr = (_ffi.TuneEntry * max(n.value, 1))()
+    check(get(arr, n.value, C.byref(n)))
+    return [{k: getattr(arr[q], k) for k, _ in _ffi.TuneEntry._fields_} for q in range(n.value)]

@@ -137,6 +137,89 @@ def test_batch_tile_shape_does_not_change_results(engine, march):
     batch.close()
 
 
+def _class_members(precision):
+    """Members spanning every tuned axis: planar and 3-D, size classes 5 to 8, x slab classes
+    0 (no CPML), 1 (up to 8 cells), 2 (up to 16) and 3 (deeper), uniform and non-uniform."""
+    from luxum_gb300 import Sim
+
+    extra = {
+        "planar_pml12": dict(isPlanar=1, Nx=96, Ny=1, Nz=96, **cases.pw((1, 0, 0), (0, 1, 0), ((18, 77), (0, 0), (18, 77))),
+                             **cases.pml(12)),
+        "3d_pml20": dict(isPlanar=0, Nx=60, Ny=58, Nz=62, **cases.pw((1, 0, 0), (0, 0, 1), ((24, 35), (23, 34), (24, 37))),
+                         **cases.pml(20, kappa=15, a_max=0.0)),
+    }
+    out = [_make(n, precision) for n in ("planar_pml_axis", "planar_oblique", "3d_pml_axis", "3d_oblique",
+                                         "3d_pml_pulse_nonuniform")]
+    for kw in extra.values():
+        p = cases.make(**kw)
+        p.precision = precision
+        out.append(Sim(p))
+    return out
+
+
+@pytest.mark.parametrize("precision", [1, 0, 2])
+def test_tune_table_classes_do_not_change_results(engine, precision):
+    """Every class of member takes its own march from the table (1, 2, 4, 8 in turn), so
+    members of one launch group split by march; results stay bit-identical to solo steps."""
+    from luxum_gb300 import Batch
+
+    members = _class_members(precision)
+    twins = _class_members(precision)
+    classes = []
+    for m in members:
+        k = m.tune_class()
+        if k not in classes:
+            classes.append(k)
+    assert {k["slab_class"] for k in classes} == {0, 1, 2, 3}
+    assert {k["planar"] for k in classes} == {0, 1}
+    assert len({k["size_class"] for k in classes}) >= 3
+    assert all(k["precision"] == precision for k in classes)
+    table = [dict(k, march=(1, 2, 4, 8)[q % 4]) for q, k in enumerate(classes)]
+    batch = Batch(chunk=10)
+    batch.set_tune_table(table)
+    assert batch.tune_table() == table
+    for m in members:
+        batch.add(m)
+    batch.step(37)
+    for t in twins:
+        t.step(37)
+    for m, t in zip(members, twins):
+        _same(m, t)
+    # the tuner records one entry per class and leaves the members' results unchanged
+    batch.set_tune_table([])
+    batch.autotune(3)
+    got = batch.tune_table()
+    assert sorted((e["planar"], e["size_class"], e["slab_class"]) for e in got) == \
+        sorted((k["planar"], k["size_class"], k["slab_class"]) for k in classes)
+    assert all(e["march"] in (1, 2, 4, 8) for e in got)
+    batch.step(11)
+    for t in twins:
+        t.step(11)
+    for m, t in zip(members, twins):
+        _same(m, t)
+    batch.close()
+
+
+def test_tune_table_validation_and_member_tuning(engine):
+    from luxum_gb300 import Batch, LuxumError
+
+    batch = Batch(chunk=10)
+    k = dict(planar=1, size_class=6, precision=1, slab_class=1)
+    with pytest.raises(LuxumError):
+        batch.set_tune_table([dict(k, march=3)])
+    with pytest.raises(LuxumError):
+        batch.set_tune_table([dict(k, slab_class=4, march=2)])
+    batch.set_tune_table([dict(k, march=2), dict(k, march=4)])  # the last entry of a class wins
+    assert batch.tune_table() == [dict(k, march=4)]
+    s = _make("planar_pml_axis", 1)
+    assert s.tune_class() == k
+    m = batch.tune_member(s, 3)
+    assert m in (1, 2, 4, 8)
+    assert batch.tune_table() == [dict(k, march=m)]
+    assert s.t == 0  # the handle itself is not stepped
+    batch.close()
+
+
 def test_batch_autotune_leaves_members_untouched(engine):
     from luxum_gb300 import Batch
 

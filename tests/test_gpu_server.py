@@ -65,6 +65,25 @@ def test_server_results_equal_solo(engine):
         st = srv.stats()
         assert st["done"] == len(REQS) and st["running"] == 0 and st["queued"] == 0
         assert st["cell_updates"] > 0 and st["bytes_running"] == pytest.approx(0.0, abs=1.0)
+        # every request's class was tuned on twins before it joined (all four are batched)
+        table = srv.tune_table()
+        classes = {(e["planar"], e["size_class"], e["slab_class"]) for e in table}
+        assert len(classes) == len(table) == st["tuned_classes"] == 4
+        assert all(e["march"] in (1, 2, 4, 8) and e["precision"] == 1 for e in table)
+        assert st["tune_seconds"] > 0
+
+
+def test_server_without_tuning_keeps_default_shapes(engine):
+    from luxum_gb300 import Server
+
+    n, steps, boxes, dft = REQS[0]
+    with Server(chunk=50, tune_steps=0) as srv:
+        rid = srv.submit(_params(n), steps, boxes, dft)
+        assert srv.wait(rid, 120.0) == "done", srv.error(rid)
+        twin, plane = _solo(n, steps, boxes, dft)
+        assert np.array_equal(srv.flux(rid), twin.dft_flux(plane))
+        assert srv.tune_table() == [] and srv.stats()["tuned_classes"] == 0
+        twin.close()
 
 
 def test_server_arrivals_while_others_run(engine):
