@@ -304,15 +304,18 @@ LX_API lx_status lx_batch_set_tune_table(lx_batch* b, const lx_tune_entry* entri
 /* Copies up to cap entries to entries (may be NULL when cap is 0); *n = the table's length. */
 LX_API lx_status lx_batch_get_tune_table(const lx_batch* b, lx_tune_entry* entries, int cap, int* n);
 /* Tunes the class of every batched member (3-D members of 2^18 cells or more and planar
- * single-sweep members are launched one by one and have no tile shape): for each class, times
- * `steps` batched steps of each march on zero-field twins of a sample of the class's members
- * (up to 1.5e8 cells, created and freed here) and records the fastest in the table.  The
- * members themselves are not stepped.  The per-dimension march becomes the pick of the
- * dimension's largest class (by cells) and is reported. */
+ * single-sweep members are launched one by one and have no tile shape).  Zero-field twins of
+ * a sample of the members (up to 1.5e8 cells, at least one per class; created and freed here)
+ * are stepped together, `steps` steps per timing: first with one march for every class, then
+ * with each class in turn (largest first) moved to each other march, a move kept when the
+ * whole sample runs 2 % faster, so that a class's pick pays for the launch it splits off.
+ * Every class's pick is recorded in the table.  The members themselves are not stepped.  The
+ * per-dimension march becomes the pick of the dimension's largest class and is reported. */
 LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* planar_rows, int* planes_3d);
 /* Tunes the class of one handle (not necessarily a member yet) on zero-field twins of it,
- * replicated up to 2^22 cells or 16 twins, and records the pick; *march = 0 when the class has
- * no tile shape.  The handle is not stepped.  Waits for the batch's enqueued steps. */
+ * replicated up to 2^22 cells or 16 twins, and records the pick; a march other than the
+ * dimension's (lx_batch_set_march) must run 5 % faster.  *march = 0 when the class has no tile
+ * shape.  The handle is not stepped.  Waits for the batch's enqueued steps. */
 LX_API lx_status lx_batch_tune_member(lx_batch* b, const lx_sim* sim, int steps, int* march);
 
 /* ---- Serving: continuous batching of submitted simulations --------------------------

@@ -2262,53 +2262,63 @@ extern "C" LX_API lx_status lx_batch_get_march(const lx_batch* b, int* planar_ro
   return LX_OK;
 }
 
-// Times `steps` batched steps of twins (zero fields, same parameters and Cb) of `sample`, each
-// member `copies` times, on a scratch batch for each march length; the sampled handles
-// themselves are not touched.  *best = the fastest march.
-static lx_status time_marches(const std::vector<const lx_sim*>& sample, int copies, int steps, int* best) {
-  *best = 0;
-  std::vector<lx_sim*> twins;
+// A scratch batch of zero-field twins (same parameters and Cb) of sampled handles, for timing
+// tile shapes; the sampled handles themselves are never stepped.
+struct TuneTwins {
   lx_batch* tb = nullptr;
-  lx_status st = lx_batch_create(&tb);
-  if (!st) st = lx_batch_set_chunk(tb, 0);
+  std::vector<lx_sim*> sims;
+  TuneTwins() = default;
+  TuneTwins(const TuneTwins&) = delete;
+  TuneTwins& operator=(const TuneTwins&) = delete;
+  ~TuneTwins() {
+    if (tb) lx_batch_destroy(tb);
+    for (auto* t : sims) lx_sim_destroy(t);
+  }
+};
+
+// Twins of `sample`, each `copies` times, as members of one scratch batch (no graphs).
+static lx_status make_twins(const std::vector<const lx_sim*>& sample, int copies, TuneTwins* tw) {
+  lx_status st = lx_batch_create(&tw->tb);
+  if (!st) st = lx_batch_set_chunk(tw->tb, 0);
   for (size_t q = 0; q < sample.size() * copies && !st; q++) {
     const lx_sim* src = sample[q % sample.size()];
     lx_sim* t = nullptr;
     st = lx_sim_create(&src->p, &t);
     if (st) break;
-    twins.push_back(t);
+    tw->sims.push_back(t);
     for (int c = 0; c < 3 && !st; c++)
       if (src->Cbs[c] && ext_n(src, c))
         if (cudaMemcpyAsync(t->Cbs[c], src->Cbs[c], t->ncell * t->csize, cudaMemcpyDeviceToDevice, t->stream) != cudaSuccess)
           st = fail(nullptr, LX_ERR_CUDA, "copying Cb to a tuning twin failed");
     if (!st) st = lx_sim_sync(t);
-    if (!st) st = lx_batch_add(tb, t);
+    if (!st) st = lx_batch_add(tw->tb, t);
   }
-  float best_ms = 0.f;
+  return st;
+}
+
+// Milliseconds for `steps` batched steps of the scratch batch with its current tile shapes:
+// a rebuild and two warm-up steps, then the better of two timed runs (CUDA events on the
+// batch stream).
+static lx_status time_steps(lx_batch* tb, int steps, float* ms) {
+  *ms = 0.f;
+  lx_status st = lx_batch_step(tb, 2);
+  if (st == LX_ERR_BLOWUP) st = LX_OK;  // zero fields cannot blow up; tolerate a source-driven twin
+  if (st) return st;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (!st && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     st = fail(nullptr, LX_ERR_CUDA, "cudaEventCreate failed");
-  const int cand[4] = {1, 2, 4, 8};
-  for (int q = 0; q < 4 && !st; q++) {
-    st = lx_batch_set_march(tb, cand[q], cand[q]);
-    if (!st) st = lx_batch_step(tb, 2);  // rebuild and warm up
-    if (st) break;
+  for (int rep = 0; rep < 2 && !st; rep++) {
     cudaEventRecord(e0, tb->stream);
     st = lx_batch_step_async(tb, steps);
     cudaEventRecord(e1, tb->stream);
     if (!st) st = lx_batch_wait(tb);
-    if (st == LX_ERR_BLOWUP) st = LX_OK;  // zero fields cannot blow up; tolerate a source-driven twin
-    float ms = 0.f;
-    if (!st && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) st = fail(nullptr, LX_ERR_CUDA, "event timing failed");
-    if (!st && (*best == 0 || ms < best_ms)) {
-      best_ms = ms;
-      *best = cand[q];
-    }
+    if (st == LX_ERR_BLOWUP) st = LX_OK;
+    float t = 0.f;
+    if (!st && cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) st = fail(nullptr, LX_ERR_CUDA, "event timing failed");
+    if (!st && (rep == 0 || t < *ms)) *ms = t;
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
-  if (tb) lx_batch_destroy(tb);
-  for (auto* t : twins) lx_sim_destroy(t);
   return st;
 }
 
@@ -2354,41 +2364,81 @@ extern "C" LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* plana
   lx::DeviceGuard dg_(b->device);
   lx_status st = lx_batch_wait(b);
   if (st) return st;
-  // the classes of the batched members, with a sample of each up to the cell budget
+  // The classes of the batched members, and a sample of them within the cell budget that holds
+  // at least one member of every class.
   const double budget = 1.5e8;
   std::vector<lx_tune_entry> classes;
-  std::vector<std::vector<const lx_sim*>> samples;
-  std::vector<double> sampled, total;
+  std::vector<double> total;
+  std::vector<const lx_sim*> sample;
+  double sampled = 0.0;
   for (auto* s : b->sims) {
     if (batch_alone(s)) continue;
     const lx_tune_entry k = tune_class_of(s);
     size_t c = 0;
     while (c < classes.size() && !same_class(classes[c], k)) c++;
-    if (c == classes.size()) {
+    const double cells = (double)s->Nx * s->Ny * s->Nz;
+    const bool first = c == classes.size();  // a class's first member is always sampled
+    if (first) {
       classes.push_back(k);
-      samples.emplace_back();
-      sampled.push_back(0.0);
       total.push_back(0.0);
     }
-    const double cells = (double)s->Nx * s->Ny * s->Nz;
     total[c] += cells;
-    if (samples[c].empty() || sampled[c] + cells <= budget) {
-      samples[c].push_back(s);
-      sampled[c] += cells;
+    if (first || sampled + cells <= budget) {
+      sample.push_back(s);
+      sampled += cells;
     }
   }
+  if (classes.empty()) {
+    if (planar_rows) *planar_rows = b->march2d;
+    if (planes_3d) *planes_3d = b->march3d;
+    return LX_OK;
+  }
+  // Time the whole sample together, so that a class's pick pays for the launch it splits off:
+  // first one march for every class, then each class in turn (largest first) moved to each
+  // other march, a move kept when it saves 2 %.
+  TuneTwins tw;
+  if ((st = make_twins(sample, 1, &tw))) return st;
+  auto timed = [&](std::vector<lx_tune_entry>& tab, float* ms) -> lx_status {
+    lx_status r = lx_batch_set_tune_table(tw.tb, tab.data(), (int)tab.size());
+    return r ? r : time_steps(tw.tb, steps, ms);
+  };
+  const int cand[4] = {1, 2, 4, 8};
+  std::vector<lx_tune_entry> cur = classes;
+  float cur_ms = 0.f;
+  for (int m : cand) {
+    std::vector<lx_tune_entry> tab = classes;
+    for (auto& e : tab) e.march = m;
+    float ms = 0.f;
+    if ((st = timed(tab, &ms))) return st;
+    if (cur_ms == 0.f || ms < cur_ms) {
+      cur_ms = ms;
+      cur = tab;
+    }
+  }
+  std::vector<size_t> order(classes.size());
+  for (size_t c = 0; c < order.size(); c++) order[c] = c;
+  std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return total[x] > total[y]; });
+  if (classes.size() > 1)
+    for (size_t c : order)
+      for (int m : cand) {
+        if (m == cur[c].march) continue;
+        std::vector<lx_tune_entry> tab = cur;
+        tab[c].march = m;
+        float ms = 0.f;
+        if ((st = timed(tab, &ms))) return st;
+        if (ms < 0.98f * cur_ms) {
+          cur_ms = ms;
+          cur = tab;
+        }
+      }
+  for (const auto& e : cur) table_put(b, e);
   int m2 = 0, m3 = 0;
   double big2 = -1.0, big3 = -1.0;
-  for (size_t c = 0; c < classes.size(); c++) {
-    int best = 0;
-    if ((st = time_marches(samples[c], 1, steps, &best))) return st;
-    if (!best) continue;
-    classes[c].march = best;
-    table_put(b, classes[c]);
-    double& big = classes[c].planar ? big2 : big3;
+  for (size_t c = 0; c < cur.size(); c++) {
+    double& big = cur[c].planar ? big2 : big3;
     if (total[c] > big) {
       big = total[c];
-      (classes[c].planar ? m2 : m3) = best;
+      (cur[c].planar ? m2 : m3) = cur[c].march;
     }
   }
   if ((st = lx_batch_set_march(b, m2 ? m2 : b->march2d, m3 ? m3 : b->march3d))) return st;
@@ -2406,16 +2456,28 @@ extern "C" LX_API lx_status lx_batch_tune_member(lx_batch* b, const lx_sim* s, i
   lx_status st = lx_batch_wait(b);
   if (st) return st;
   if (batch_alone(s)) return LX_OK;
+  // Twins of the handle alone (replicated to a few launches' worth of work): a pick other than
+  // the dimension's march must save 5 %, since members of one launch group split by march.
   const double cells = (double)s->Nx * s->Ny * s->Nz;
   const int copies = (int)std::max(1.0, std::min(16.0, std::floor(4194304.0 / std::max(cells, 1.0))));
-  int best = 0;
-  if ((st = time_marches({s}, copies, steps, &best))) return st;
-  if (best) {
-    lx_tune_entry e = tune_class_of(s);
-    e.march = best;
-    table_put(b, e);
-    batch_reshape(b);
+  TuneTwins tw;
+  if ((st = make_twins({s}, copies, &tw))) return st;
+  const int def = s->planar ? b->march2d : b->march3d;
+  const int cand[4] = {1, 2, 4, 8};
+  float t[4] = {}, t_def = 0.f;
+  int bq = 0;
+  for (int q = 0; q < 4; q++) {
+    if ((st = lx_batch_set_march(tw.tb, cand[q], cand[q]))) return st;
+    if ((st = time_steps(tw.tb, steps, &t[q]))) return st;
+    if (cand[q] == def) t_def = t[q];
+    if (t[q] < t[bq]) bq = q;
   }
+  int best = cand[bq];
+  if (best != def && t[bq] > 0.95f * t_def) best = def;
+  lx_tune_entry e = tune_class_of(s);
+  e.march = best;
+  table_put(b, e);
+  batch_reshape(b);
   if (march) *march = best;
   return LX_OK;
 }
