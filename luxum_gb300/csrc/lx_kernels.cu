@@ -16,6 +16,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <cstring>
 
 #include "lx_device.cuh"
@@ -244,24 +245,28 @@ struct HMinBlocks {
   static constexpr int v = sizeof(C) == 4 ? 8 : 5;
 };
 
-// The z cells of a 3-D block.  Plain tiles are 32 consecutive cells.  With zends (FP64 grids
-// whose z CPML slabs are at most 16 cells wide), tile 0 is the row's two ends, k in [0, 16)
-// and [Nz-16, Nz), and tile m > 0 is [16 + 32(m-1), +32) up to Nz-16.  A plain row's first
-// and last tiles are half slab, and their warps run the z psi code with half the lanes idle;
-// the end tile runs it once with all lanes busy, and sixteen doubles keep the other tiles on
-// 128-byte lines.  Each lane has one cell (valid = inside its tile's range).
+// The z cells of a 3-D block.  Plain tiles are ZW consecutive cells (32, or 16 for float
+// storage: a block is ZW z cells x 256/ZW y rows).  With zends (FP64 grids whose z CPML slabs
+// are at most 16 cells wide; ZW = 32), tile 0 is the row's two ends, k in [0, 16) and
+// [Nz-16, Nz), and tile m > 0 is [16 + 32(m-1), +32) up to Nz-16.  A 32-cell row's first and
+// last tiles are half slab, and their warps run the z psi code with half the lanes idle; the
+// end tile runs it once with all lanes busy, and sixteen doubles keep the other tiles on
+// 128-byte lines.  Sixteen floats are half a line, so float storage takes 16-cell tiles
+// instead: its slab tiles are whole slab, and half as many.  Each thread has one cell
+// (valid = inside its tile's range).
 struct ZTile {
   int k;
   bool valid;
   int lo0, n0, lo1, n1;  // the tile's cells: [lo0, lo0+n0) and [lo1, lo1+n1)
 };
 
+template <int ZW>
 __device__ __forceinline__ ZTile z_tile(int Nz, bool ends) {
   ZTile z;
   const int lane = threadIdx.x;
-  if (!ends) {
-    z.lo0 = blockIdx.x * 32;
-    z.n0 = 32;
+  if (ZW != 32 || !ends) {
+    z.lo0 = blockIdx.x * ZW;
+    z.n0 = ZW;
     z.lo1 = z.n1 = 0;
     z.k = z.lo0 + lane;
     z.valid = z.k < Nz;
@@ -282,22 +287,23 @@ __device__ __forceinline__ ZTile z_tile(int Nz, bool ends) {
   return z;
 }
 
-// Whether a 3-D block's tile meets a TF/SF plane, and whether it is interior.
-__device__ __forceinline__ bool ztile_meets_planes(const int (&pl)[3][2], int i, int j0, const ZTile& z) {
-  return tile_meets_planes(pl, i, 1, j0, 8, z.lo0, z.n0) || (z.n1 > 0 && tile_meets_planes(pl, i, 1, j0, 8, z.lo1, z.n1));
+// Whether a 3-D block's tile (rows [j0, j0+nj)) meets a TF/SF plane.
+__device__ __forceinline__ bool ztile_meets_planes(const int (&pl)[3][2], int i, int j0, int nj, const ZTile& z) {
+  return tile_meets_planes(pl, i, 1, j0, nj, z.lo0, z.n0) || (z.n1 > 0 && tile_meets_planes(pl, i, 1, j0, nj, z.lo1, z.n1));
 }
 
-// One cell per thread; a block is 32 (z) x 8 (y) cells of one x plane.  Blocks whose tile is
-// interior take the cell code with every condition decided at compile time.
-template <class T, class C, bool UNI>
+// One cell per thread; a block is ZW (z) x 256/ZW (y) cells of one x plane.  Blocks whose tile
+// is interior take the cell code with every condition decided at compile time.
+template <class T, class C, bool UNI, int ZW>
 __global__ void __launch_bounds__(256, HMinBlocks<C>::v) h_kernel_3d(const StepParams<T, C> p) {
-  const ZTile z = z_tile(p.Nz, p.zends);
+  constexpr int RY = 256 / ZW;
+  const ZTile z = z_tile<ZW>(p.Nz, p.zends);
   const int k = z.k;
-  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int j = blockIdx.y * RY + threadIdx.y;
   const int i = blockIdx.z;
   if (!z.valid || j >= p.Ny) return;
-  const bool tf = p.tfsf && ztile_meets_planes(p.planesH, i, blockIdx.y * 8, z);
-  if (!tf && z.n1 == 0 && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * 8, 8, z.lo0, z.n0))
+  const bool tf = p.tfsf && ztile_meets_planes(p.planesH, i, blockIdx.y * RY, RY, z);
+  if (!tf && z.n1 == 0 && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * RY, RY, z.lo0, z.n0))
     h_cell_3d<T, C, UNI, true>(p, i, j, k, false);
   else
     h_cell_3d<T, C, UNI>(p, i, j, k, tf);
@@ -416,19 +422,20 @@ __device__ __forceinline__ typename MaxBits<C>::type e_cell_3d(const StepParams<
   return e_apply<T, C, UNI, MON, FAST>(p, i, j, k, tf, v);
 }
 
-template <class T, class C, bool UNI, bool MON>
+template <class T, class C, bool UNI, bool MON, int ZW>
 __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
-  const ZTile z = z_tile(p.Nz, p.zends);
+  constexpr int RY = 256 / ZW;
+  const ZTile z = z_tile<ZW>(p.Nz, p.zends);
   const int k = z.k;
-  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int j = blockIdx.y * RY + threadIdx.y;
   const int i = blockIdx.z;
-  const bool tf = p.tfsf && ztile_meets_planes(p.planesE, i, blockIdx.y * 8, z);
+  const bool tf = p.tfsf && ztile_meets_planes(p.planesE, i, blockIdx.y * RY, RY, z);
   typename MaxBits<C>::type mbits = 0;
   // The interior fast path pays for FP32 storage only (1.5 %); FP64 is bound by its pipe
   // either way, and FP16 storage ran 9 % slower with it.
   constexpr bool kFast = sizeof(T) == 4;
   if (z.valid && j < p.Ny) {
-    if (kFast && !tf && z.n1 == 0 && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * 8, 8, z.lo0, z.n0))
+    if (kFast && !tf && z.n1 == 0 && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * RY, RY, z.lo0, z.n0))
       mbits = e_cell_3d<T, C, UNI, MON, kFast>(p, i, j, k, false);
     else
       mbits = e_cell_3d<T, C, UNI, MON>(p, i, j, k, tf);
@@ -1146,6 +1153,16 @@ cudaError_t launch_prologue(const PrologueParams& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// 16-cell z tiles for the 3-D E kernel with float storage (default); LUXUM_ZTILE=32 keeps the
+// 32-cell tiles, read once per process.
+static bool z16_tiles() {
+  static const bool on = [] {
+    const char* v = std::getenv("LUXUM_ZTILE");
+    return !(v && std::strcmp(v, "32") == 0);
+  }();
+  return on;
+}
+
 template <class T, class C>
 cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bool h_half, cudaStream_t s) {
   // single simulations: one cell per thread (their parameters sit in the constant bank, and
@@ -1165,20 +1182,34 @@ cudaError_t launch_step(const StepParams<T, C>& p, bool planar, bool uniform, bo
       else e_kernel_2d<T, C, false, false><<<grid, block, 0, s>>>(p);
     }
   } else {
-    // FP64 with z CPML slabs of at most 16 cells: the rows' two ends share one tile (ZTile)
+    // FP64 with z CPML slabs of at most 16 cells: the rows' two ends share one tile (ZTile).
+    // The E kernel with float storage takes 16-cell z tiles (LUXUM_ZTILE=32 keeps 32): on the
+    // 256^3 drop-in grid E 0.2035 -> 0.189 ms (FP32), 0.200 -> 0.187 (FP16 storage), from its
+    // CPML and TF/SF tiles; the H kernel ran 0.015 ms slower with them, CPML or not.
     StepParams<T, C> q = p;
     q.zends = sizeof(T) == 8 && p.pml && p.slab[2].n > 0 && p.slab[2].lo <= 16 && p.Nz - p.slab[2].hi0 <= 16 &&
               p.Nz >= 48;
+    if (sizeof(T) < 8 && !h_half && z16_tiles()) {
+      const dim3 block16(16, 16), grid16((p.Nz + 15) / 16, (p.Ny + 15) / 16, p.Nx);
+      if (mon) {
+        if (uniform) e_kernel_3d<T, C, true, true, 16><<<grid16, block16, 0, s>>>(q);
+        else e_kernel_3d<T, C, false, true, 16><<<grid16, block16, 0, s>>>(q);
+      } else {
+        if (uniform) e_kernel_3d<T, C, true, false, 16><<<grid16, block16, 0, s>>>(q);
+        else e_kernel_3d<T, C, false, false, 16><<<grid16, block16, 0, s>>>(q);
+      }
+      return cudaGetLastError();
+    }
     dim3 grid(q.zends ? 1 + (p.Nz - 32 + 31) / 32 : (p.Nz + 31) / 32, (p.Ny + 7) / 8, p.Nx);
     if (h_half) {
-      if (uniform) h_kernel_3d<T, C, true><<<grid, block, 0, s>>>(q);
-      else h_kernel_3d<T, C, false><<<grid, block, 0, s>>>(q);
+      if (uniform) h_kernel_3d<T, C, true, 32><<<grid, block, 0, s>>>(q);
+      else h_kernel_3d<T, C, false, 32><<<grid, block, 0, s>>>(q);
     } else if (mon) {
-      if (uniform) e_kernel_3d<T, C, true, true><<<grid, block, 0, s>>>(q);
-      else e_kernel_3d<T, C, false, true><<<grid, block, 0, s>>>(q);
+      if (uniform) e_kernel_3d<T, C, true, true, 32><<<grid, block, 0, s>>>(q);
+      else e_kernel_3d<T, C, false, true, 32><<<grid, block, 0, s>>>(q);
     } else {
-      if (uniform) e_kernel_3d<T, C, true, false><<<grid, block, 0, s>>>(q);
-      else e_kernel_3d<T, C, false, false><<<grid, block, 0, s>>>(q);
+      if (uniform) e_kernel_3d<T, C, true, false, 32><<<grid, block, 0, s>>>(q);
+      else e_kernel_3d<T, C, false, false, 32><<<grid, block, 0, s>>>(q);
     }
   }
   return cudaGetLastError();
