@@ -568,7 +568,57 @@ def serve_params(req):
     return params(isPlanar=0, Nx=n, Ny=n, Nz=n, Ez_pw=1.0, **kw)
 
 
-def run_serve(n_requests: int, rate: float, budget_gb: float, chunk: int, peak: float, peak_kind: str) -> dict:
+SERVE_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "luxum_gb300", "serve_tile_shapes.json")
+
+
+def load_serve_table():
+    """The committed tile-shape table of the serving stream's request classes (empty if absent)."""
+    if not os.path.exists(SERVE_TABLE):
+        return []
+    with open(SERVE_TABLE) as f:
+        return json.load(f)["table"]
+
+
+def bench_serve_tune(args):
+    """--config serve-tune: writes the serving stream's tile-shape table (serve_table) to
+    SERVE_TABLE.  Run in a process of its own: tuning in the serving process slowed the stream
+    that followed (47 against 55 Gcell/s on 1000 requests), whether or not its table was used."""
+    import __graft_entry__
+
+    __graft_entry__.build()
+    reqs = serve_requests(args.serve_requests, 5, args.serve_rate)
+    table, seconds = serve_table(reqs)
+    with open(SERVE_TABLE, "w") as f:
+        json.dump({"table": table, "tuned_on": "twins of the first 64 requests of the seeded serving stream "
+                   "(lx_batch_autotune, 10 steps per timing)", "seconds": round(seconds, 3)}, f, indent=1)
+        f.write("\n")
+    print(json.dumps({"table": table, "seconds": seconds, "path": SERVE_TABLE}), flush=True)
+
+
+def serve_table(reqs, n: int = 64, steps: int = 10):
+    """Tile shapes per request class for the server: lx_batch_autotune on twins of the stream's
+    first n requests (a fixed sample), before the stream starts.  Returns (table, seconds)."""
+    from luxum_gb300 import Batch, Sim
+
+    t0 = time.perf_counter()
+    sims = []
+    b = Batch(chunk=0)
+    for r in reqs[:n]:
+        s = Sim(serve_params(r))
+        for lo, hi, eps in r["boxes"]:
+            s.set_eps_box(lo, hi, eps)
+        b.add(s)
+        sims.append(s)
+    b.autotune(steps)
+    table = b.tune_table()
+    b.close()
+    for s in sims:
+        s.close()
+    return table, time.perf_counter() - t0
+
+
+def run_serve(n_requests: int, rate: float, budget_gb: float, chunk: int, peak: float, peak_kind: str,
+              tune_steps: int | None = None) -> dict:
     """A Poisson request stream through the native server (lx_server_*): continuous batching
     under an HBM budget, latency taken by the server's own clock."""
     import torch
@@ -576,7 +626,9 @@ def run_serve(n_requests: int, rate: float, budget_gb: float, chunk: int, peak: 
     from luxum_gb300 import LX_PREC_FP32, Server, step_bytes
 
     reqs = serve_requests(n_requests, 5, rate)
-    srv = Server(precision=LX_PREC_FP32, chunk=chunk, budget_bytes=budget_gb * 1e9)
+    table = load_serve_table()
+    srv = Server(precision=LX_PREC_FP32, chunk=chunk, budget_bytes=budget_gb * 1e9, tune_steps=tune_steps,
+                 tune_table=table)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ids = []
@@ -617,9 +669,11 @@ def run_serve(n_requests: int, rate: float, budget_gb: float, chunk: int, peak: 
             "sustained": bool(work / wall / 1e9 >= 0.95 * offered),
             "peak_running": st["peak_running"], "peak_budget_gb": st["peak_bytes_running"] / 1e9,
             "chunks": st["chunks"], "gpu_busy_s": st["busy_seconds"],
-            "tuned_march": {"table": table, "seconds": st["tune_seconds"],
-                            "note": "tile shape per request class, tuned on twins of its first request before it "
-                                    "joined (inside the stream's wall time)"},
+            "worker_seconds": {k: st[k + "_seconds"] for k in ("enqueue", "prepare", "wait", "join", "retire", "tune")},
+            "tuned_march": {"table": table, "source": SERVE_TABLE, "seconds_online": st["tune_seconds"],
+                            "note": "tile shape per request class, from lx_batch_autotune on twins of the stream's "
+                                    "first 64 requests (bench.py --config serve-tune, its own process), given to the "
+                                    "server at creation; classes tuned online while serving (tune_steps) add to it"},
             "dtype": "f32", "clocks": clk.summary()}
 
 
@@ -630,7 +684,7 @@ def bench_serve(args):
     __graft_entry__.build()
     peak, kind = measured_peaks()
     print(json.dumps(run_serve(args.serve_requests, args.serve_rate, args.serve_budget_gb, args.serve_chunk, peak,
-                               kind)), flush=True)
+                               kind, args.serve_tune_steps)), flush=True)
 
 
 PHC = dict(nx=512, ny=512, nz=128, steps=4000, cpml=20, period=40, rod=16, eps=12.0)
@@ -880,7 +934,7 @@ def main():
     ap.add_argument("--profile-io", action="store_true", help="profiling case (3-D): probes and snapshots too")
     ap.add_argument("--batch-side-lo", type=int, default=64, help="batch3d: smallest cube side")
     ap.add_argument("--batch-side-hi", type=int, default=192, help="batch3d: largest cube side")
-    ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "batch3d", "serve", "phc"],
+    ap.add_argument("--config", default="drop-in", choices=["drop-in", "batch", "batch3d", "serve", "serve-tune", "phc"],
                     help="drop-in: the headline 256^3 FP64 workload; batch: 256 uneven planar simulations")
     ap.add_argument("--batch-sims", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=3000)
@@ -890,11 +944,15 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-chunk", type=int, default=100)
+    ap.add_argument("--serve-tune-steps", type=int, default=None,
+                    help="steps per march when the server tunes a new request class (0: default tile shapes)")
     args = ap.parse_args()
     if args.config in ("batch", "batch3d"):
         if args.config == "batch3d" and args.batch_sims == 256:
             args.batch_sims, args.batch_steps = 48, 1000
         return bench_batch(args)
+    if args.config == "serve-tune":
+        return bench_serve_tune(args)
     if args.config == "serve":
         return bench_serve(args)
     if args.config == "phc":

@@ -144,6 +144,10 @@ LX_API lx_status lx_params_device_bytes(const lx_params* p, size_t* bytes);
  * sizes of p->precision.  The figure a roofline divides by the step time.  Measurement aid
  * with no counterpart in the reference (whose drivers move about four times as much). */
 LX_API lx_status lx_params_step_bytes(const lx_params* p, double* bytes);
+/* Handles and batches take device memory from the current device's stream-ordered pool and
+ * give it back there when destroyed, for reuse without a device-wide synchronisation.  This
+ * waits for the device and returns the pool's unused memory to the driver. */
+LX_API lx_status lx_trim_device_memory(void);
 /* Zeroes E, H, psi and |E|^2 and rewinds to step 0 (the state after lx_sim_create); keeps
  * Cb, probe positions and snapshot outputs, so one handle can run many simulations. */
 LX_API lx_status lx_sim_reset(lx_sim* sim);
@@ -313,7 +317,7 @@ LX_API lx_status lx_batch_get_tune_table(const lx_batch* b, lx_tune_entry* entri
  * per-dimension march becomes the pick of the dimension's largest class and is reported. */
 LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* planar_rows, int* planes_3d);
 /* Tunes the class of one handle (not necessarily a member yet) on zero-field twins of it,
- * replicated up to 2^22 cells or 16 twins, and records the pick; a march other than the
+ * replicated up to 2^24 cells or 64 twins, and records the pick; a march other than the
  * dimension's (lx_batch_set_march) must run 5 % faster.  *march = 0 when the class has no tile
  * shape.  The handle is not stepped.  Waits for the batch's enqueued steps. */
 LX_API lx_status lx_batch_tune_member(lx_batch* b, const lx_sim* sim, int steps, int* march);
@@ -334,7 +338,11 @@ typedef struct lx_server_config {
   int max_running;        /* 0: no limit besides the budget */
   int tune_steps;         /* > 0: tune each new class of batched request on twins of it before
                              it joins (lx_batch_tune_member, `tune_steps` steps per march);
-                             0: the default tile shapes (default 10) */
+                             0 (default): no tuning while serving */
+  const lx_tune_entry* tune_table;  /* tile shapes per request class to start from (copied at
+                                       creation; e.g. from lx_batch_autotune on a sample of the
+                                       expected requests), or NULL */
+  int tune_entries;
 } lx_server_config;
 LX_API void lx_server_config_init(lx_server_config* cfg);
 
@@ -367,6 +375,10 @@ typedef struct lx_server_stats {
   long long chunks;
   double tune_seconds;        /* worker time spent tuning classes (outside busy_seconds) */
   int tuned_classes;
+  /* where the worker's time goes (seconds): enqueueing chunks (batch rebuilds and graph
+   * captures included), creating request handles (inside chunks and between them), waiting
+   * for chunks to finish after that, adding prepared handles to the batch, retiring requests */
+  double enqueue_seconds, prepare_seconds, wait_seconds, join_seconds, retire_seconds;
 } lx_server_stats;
 
 LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_server** out);

@@ -7,7 +7,8 @@ line driver `luxum` and the C ABI are the other two.
 from ._ffi import (COMPONENTS, ETOTAL, EX, EY, EZ, HX, HY, HZ, LX_CPML_REFERENCE, LX_CPML_STANDARD, LX_PREC_FP16S,
                    LX_PREC_FP32, LX_PREC_FP64, LX_SRC_CW_HARD, LX_SRC_PULSE_SOFT, LuxumError, Params)
 from .server import Server
-from .sim import Batch, Sim, device_bytes, field_shape, hdf5_read, hdf5_write, params, read_yaml, step_bytes
+from .sim import (Batch, Sim, device_bytes, field_shape, hdf5_read, hdf5_write, params, read_yaml, step_bytes,
+                  trim_device_memory)
 
 __all__ = ["Batch", "Server", "Sim", "device_bytes", "step_bytes", "field_shape", "params", "read_yaml", "hdf5_read", "hdf5_write", "Params", "LuxumError", "COMPONENTS", "EX", "EY", "EZ", "HX", "HY", "HZ",
            "ETOTAL", "LX_PREC_FP64", "LX_PREC_FP32", "LX_PREC_FP16S", "LX_CPML_REFERENCE", "LX_CPML_STANDARD",

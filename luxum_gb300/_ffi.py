@@ -61,14 +61,14 @@ class Info(C.Structure):
                 ("psi_e_entries", C.c_size_t), ("slab", C.c_int * 3), ("uniform", C.c_int), ("field_bytes", C.c_int)]
 
 
-class ServerConfig(C.Structure):
-    _fields_ = [("precision", C.c_int), ("chunk", C.c_int), ("budget_bytes", C.c_double), ("max_running", C.c_int),
-                ("tune_steps", C.c_int)]
-
-
 class TuneEntry(C.Structure):
     _fields_ = [("planar", C.c_int), ("size_class", C.c_int), ("precision", C.c_int), ("slab_class", C.c_int),
                 ("march", C.c_int)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("precision", C.c_int), ("chunk", C.c_int), ("budget_bytes", C.c_double), ("max_running", C.c_int),
+                ("tune_steps", C.c_int), ("tune_table", C.POINTER(TuneEntry)), ("tune_entries", C.c_int)]
 
 
 class Request(C.Structure):
@@ -83,7 +83,9 @@ class ServerStats(C.Structure):
                 ("done", C.c_longlong), ("failed", C.c_longlong), ("cancelled", C.c_longlong),
                 ("bytes_running", C.c_double), ("peak_bytes_running", C.c_double), ("peak_running", C.c_int),
                 ("cell_updates", C.c_double), ("busy_seconds", C.c_double), ("chunks", C.c_longlong),
-                ("tune_seconds", C.c_double), ("tuned_classes", C.c_int)]
+                ("tune_seconds", C.c_double), ("tuned_classes", C.c_int), ("enqueue_seconds", C.c_double),
+                ("prepare_seconds", C.c_double), ("wait_seconds", C.c_double), ("join_seconds", C.c_double),
+                ("retire_seconds", C.c_double)]
 
 
 SNAPSHOT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int))
@@ -172,6 +174,7 @@ def declare(lib) -> None:
     _proto(lib, "lx_server_tune_table", C.c_int, srv, P(TuneEntry), C.c_int, P(C.c_int))
     _proto(lib, "lx_host_alloc", C.c_int, C.c_size_t, P(C.c_void_p))
     _proto(lib, "lx_host_free", None, C.c_void_p)
+    _proto(lib, "lx_trim_device_memory", C.c_int)
     _proto(lib, "lx_last_error", C.c_char_p, sim)
     _proto(lib, "lx_version", C.c_char_p)
 

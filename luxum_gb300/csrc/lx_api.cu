@@ -50,9 +50,45 @@ static void keep_pool_memory() {
   done = true;
 }
 
+extern "C" LX_API lx_status lx_trim_device_memory(void) {
+  int dev = 0;
+  cudaMemPool_t pool;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+  if (e == cudaSuccess) e = cudaMemPoolTrimTo(pool, 0);
+  if (e != cudaSuccess) return lx::set_thread_error((std::string("lx_trim_device_memory: ") + cudaGetErrorString(e)).c_str(), LX_ERR_CUDA);
+  return LX_OK;
+}
+
 static void dfree(void* p, cudaStream_t st) {
   if (p) cudaFreeAsync(p, st);
 }
+
+// Reserved bytes of the device's default pool at construction; on destruction the pool is
+// trimmed back to them.  Tuning creates and frees thousands of twin allocations: left in the
+// pool, they slowed every later handle creation of the serving loop threefold (5 -> 14 s of
+// worker time over a 1000-request stream).
+class PoolMark {
+ public:
+  PoolMark() {
+    int dev = 0;
+    uint64_t v = 0;
+    ok_ = cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool_, dev) == cudaSuccess &&
+          cudaMemPoolGetAttribute(pool_, cudaMemPoolAttrReservedMemCurrent, &v) == cudaSuccess;
+    keep_ = (size_t)v;
+  }
+  ~PoolMark() {
+    if (ok_) cudaMemPoolTrimTo(pool_, keep_);
+  }
+  PoolMark(const PoolMark&) = delete;
+  PoolMark& operator=(const PoolMark&) = delete;
+
+ private:
+  cudaMemPool_t pool_ = nullptr;
+  size_t keep_ = 0;
+  bool ok_ = false;
+};
 
 static lx_status fail(lx_sim* s, lx_status st, const std::string& msg) {
   if (s) s->err = msg;
@@ -596,7 +632,12 @@ extern "C" LX_API lx_status lx_sim_create(const lx_params* p, lx_sim** out) {
   setup_host(s, p);
   cudaGetDevice(&s->device);
 
-  cudaError_t e = cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking);
+  // The handle's own stream takes the device's highest priority: what a new handle queues
+  // while a batch chunk runs (its allocations' memsets, boxes, DFT set-up, in the serving loop)
+  // is then scheduled ahead of the chunk's pending blocks rather than behind them.
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  cudaError_t e = cudaStreamCreateWithPriority(&s->own, cudaStreamNonBlocking, prio_hi);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     std::string m = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
@@ -2396,6 +2437,7 @@ extern "C" LX_API lx_status lx_batch_autotune(lx_batch* b, int steps, int* plana
   // Time the whole sample together, so that a class's pick pays for the launch it splits off:
   // first one march for every class, then each class in turn (largest first) moved to each
   // other march, a move kept when it saves 2 %.
+  PoolMark mark;  // destroyed after the twins: the pool gives their memory back
   TuneTwins tw;
   if ((st = make_twins(sample, 1, &tw))) return st;
   auto timed = [&](std::vector<lx_tune_entry>& tab, float* ms) -> lx_status {
@@ -2456,10 +2498,14 @@ extern "C" LX_API lx_status lx_batch_tune_member(lx_batch* b, const lx_sim* s, i
   lx_status st = lx_batch_wait(b);
   if (st) return st;
   if (batch_alone(s)) return LX_OK;
-  // Twins of the handle alone (replicated to a few launches' worth of work): a pick other than
-  // the dimension's march must save 5 %, since members of one launch group split by march.
+  // Twins of the handle alone, replicated to 2^24 cells or 64 twins: a batch of hundreds of
+  // members fills the GPU many times over, and a sample that fills it once or less favours
+  // short marches (16 twins of a 300^2 lens picked 2 where the full batch runs best at 8).
+  // A pick other than the dimension's march must save 5 %, since members of one launch group
+  // split by march.
   const double cells = (double)s->Nx * s->Ny * s->Nz;
-  const int copies = (int)std::max(1.0, std::min(16.0, std::floor(4194304.0 / std::max(cells, 1.0))));
+  const int copies = (int)std::max(1.0, std::min(64.0, std::floor(16777216.0 / std::max(cells, 1.0))));
+  PoolMark mark;  // destroyed after the twins: the pool gives their memory back
   TuneTwins tw;
   if ((st = make_twins({s}, copies, &tw))) return st;
   const int def = s->planar ? b->march2d : b->march3d;

@@ -871,7 +871,10 @@ __global__ void __launch_bounds__(256, B3MinBlocks<C>::v) e_batch_3d(const StepP
 
 // planar members: a block is 32 z cells x 8*M x rows.  Rows are walked one after the
 // other: issuing all rows' loads first doubles the registers, halves the resident blocks and
-// ran 25 % slower.
+// ran 25 % slower.  Interior tiles issue the next row's loads before the current row's update
+// and stores: two rows in flight per thread at the same 32 registers (each row's cells are
+// written only by their own thread, and the rows are 8 apart); the 256-lens batch ran 103 ->
+// 111 Gcell/s.  The same in the general tiles took 46-48 registers and ran 90.
 template <class T, class C, bool UNI, int M>
 __global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
@@ -880,29 +883,50 @@ __global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __rest
   if (k >= p.Nz) return;
   const bool tf = p.tfsf && tile_meets_planes(p.planesH, tl.y, 8 * M, 0, 1, tl.w, 32);
   const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, tl.y, 8 * M, tl.w, 32);
+  if (fast) {
+    const int i0 = tl.y + threadIdx.y;
+    HCell2<C> v[2];
+    h2_load<T, C, true>(p, i0, k, v[0]);
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      if (r + 1 < M) h2_load<T, C, true>(p, i0 + 8 * (r + 1), k, v[(r + 1) & 1]);
+      h2_apply<T, C, UNI, true>(p, i0 + 8 * r, k, false, v[r & 1]);
+    }
+    return;
+  }
 #pragma unroll 1
   for (int r = 0; r < M; ++r) {
     const int i = tl.y + threadIdx.y + 8 * r;
-    if (fast) h_cell_2d<T, C, UNI, true>(p, i, k, false);
-    else if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
+    if (i < p.Nx) h_cell_2d<T, C, UNI>(p, i, k, tf);
   }
 }
 
+// (Capped at 8 blocks per SM, 32 registers: left to itself the compiler took 40 for this
+// kernel once the interior path prefetched, which leaves 6 blocks.)
 template <class T, class C, bool UNI, int M>
-__global__ void __launch_bounds__(256) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
+__global__ void __launch_bounds__(256, 8) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x;
   const bool tf = p.tfsf && tile_meets_planes(p.planesE, tl.y, 8 * M, 0, 1, tl.w, 32);
   const bool fast = !tf && tile_is_interior_2d(p.slab, p.pml, p.Nx, p.Nz, tl.y, 8 * M, tl.w, 32);
   typename MaxBits<C>::type mbits = 0;
-  if (k < p.Nz) {
+  if (fast && k < p.Nz) {  // interior tile: the next row's loads first (see h_batch_2d)
+    const int i0 = tl.y + threadIdx.y;
+    ECell2<C> v[2];
+    e2_load<T, C, true, true>(p, i0, k, v[0]);
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      if (r + 1 < M) e2_load<T, C, true, true>(p, i0 + 8 * (r + 1), k, v[(r + 1) & 1]);
+      const typename MaxBits<C>::type b = e2_apply<T, C, UNI, true, true>(p, i0 + 8 * r, k, false, v[r & 1]);
+      mbits = b > mbits ? b : mbits;
+    }
+  } else if (k < p.Nz) {
 #pragma unroll 1
     for (int r = 0; r < M; ++r) {
       const int i = tl.y + threadIdx.y + 8 * r;
       typename MaxBits<C>::type b = 0;
-      if (fast) b = e_cell_2d<T, C, UNI, true, true>(p, i, k, false);
-      else if (i < p.Nx) b = e_cell_2d<T, C, UNI, true>(p, i, k, tf);
+      if (i < p.Nx) b = e_cell_2d<T, C, UNI, true>(p, i, k, tf);
       mbits = b > mbits ? b : mbits;
     }
   }

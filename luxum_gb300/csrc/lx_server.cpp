@@ -262,13 +262,19 @@ void retire(lx_server* srv) {
 
 void worker_main(lx_server* srv) {
   cudaSetDevice(srv->device);
+  auto since = [](Clock::time_point t) { return std::chrono::duration<double>(Clock::now() - t).count(); };
   for (;;) {
+    auto t0 = Clock::now();
     prepare(srv);
+    const double dp = since(t0);
     tune_prepared(srv);
     int n = 0;
     {
       std::unique_lock<std::mutex> lk(srv->mu);
+      srv->stats.prepare_seconds += dp;
+      t0 = Clock::now();
       join(srv);
+      srv->stats.join_seconds += since(t0);
       if (srv->stop) break;
       if (srv->running.empty()) {
         if (srv->queue.empty()) srv->work_cv.wait(lk, [&] { return srv->stop || !srv->queue.empty(); });
@@ -279,11 +285,19 @@ void worker_main(lx_server* srv) {
     }
     const auto c0 = Clock::now();
     lx_status st = n > 0 ? lx_batch_step_async(srv->batch, n) : LX_OK;
+    const double ds = since(c0);
+    t0 = Clock::now();
     if (!st) prepare(srv);  // next handles are created while the chunk runs
+    const double dp2 = since(t0);
+    t0 = Clock::now();
     const lx_status wst = lx_batch_wait(srv->batch);
+    const double dw = since(t0);
     if (!st) st = wst;
     std::unique_lock<std::mutex> lk(srv->mu);
-    srv->stats.busy_seconds += std::chrono::duration<double>(Clock::now() - c0).count();
+    srv->stats.busy_seconds += since(c0);
+    srv->stats.enqueue_seconds += ds;
+    srv->stats.prepare_seconds += dp2;
+    srv->stats.wait_seconds += dw;
     srv->stats.chunks += 1;
     if (st && st != LX_ERR_BLOWUP) {
       // a CUDA failure of the shared chunk fails every request in it
@@ -303,7 +317,9 @@ void worker_main(lx_server* srv) {
       r->done += n;
       srv->stats.cell_updates += r->cells * n;
     }
+    t0 = Clock::now();
     retire(srv);
+    srv->stats.retire_seconds += since(t0);
   }
   // stopping: cancel what is left
   std::unique_lock<std::mutex> lk(srv->mu);
@@ -336,7 +352,6 @@ extern "C" LX_API void lx_server_config_init(lx_server_config* cfg) {
   std::memset(cfg, 0, sizeof *cfg);
   cfg->precision = LX_PREC_FP32;
   cfg->chunk = 100;
-  cfg->tune_steps = 10;
 }
 
 extern "C" LX_API void lx_request_init(lx_request* r) {
@@ -354,7 +369,9 @@ extern "C" LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_ser
   if (cfg) c = *cfg;
   if (c.precision < LX_PREC_FP64 || c.precision > LX_PREC_FP16S) return sfail(LX_ERR_INVALID, "bad precision");
   if (c.chunk < 1) return sfail(LX_ERR_INVALID, "chunk must be >= 1");
-  if (c.max_running < 0 || c.budget_bytes < 0 || c.tune_steps < 0) return sfail(LX_ERR_INVALID, "negative limit");
+  if (c.max_running < 0 || c.budget_bytes < 0 || c.tune_steps < 0 || c.tune_entries < 0)
+    return sfail(LX_ERR_INVALID, "negative limit");
+  if (c.tune_entries > 0 && !c.tune_table) return sfail(LX_ERR_INVALID, "tune_entries without tune_table");
   if (c.budget_bytes == 0) {
     size_t fr = 0, tot = 0;
     const cudaError_t e = cudaMemGetInfo(&fr, &tot);
@@ -369,6 +386,15 @@ extern "C" LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_ser
   std::memset(&srv->stats, 0, sizeof srv->stats);
   lx_status st = lx_batch_create(&srv->batch);
   if (!st) st = lx_batch_set_chunk(srv->batch, c.chunk);
+  if (!st && c.tune_entries > 0) {
+    st = lx_batch_set_tune_table(srv->batch, c.tune_table, c.tune_entries);
+    if (!st) {
+      srv->table.assign(c.tune_table, c.tune_table + c.tune_entries);
+      for (const auto& e : srv->table) srv->tried.insert({e.planar, e.size_class, e.precision, e.slab_class});
+    }
+  }
+  srv->cfg.tune_table = nullptr;  // copied: the caller's array need not outlive the call
+  srv->cfg.tune_entries = 0;
   if (st) {
     if (srv->batch) lx_batch_destroy(srv->batch);
     delete srv;

@@ -20,13 +20,20 @@ STATES = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancelled"}
 
 class Server:
     def __init__(self, precision: int = _ffi.LX_PREC_FP32, chunk: int = 100, budget_bytes: float = 0.0,
-                 max_running: int = 0, tune_steps: int | None = None):
+                 max_running: int = 0, tune_steps: int | None = None, tune_table=None):
         self.lib = _ffi.lib()
         cfg = ServerConfig()
         self.lib.lx_server_config_init(C.byref(cfg))
         cfg.precision, cfg.chunk, cfg.budget_bytes, cfg.max_running = precision, chunk, budget_bytes, max_running
         if tune_steps is not None:
             cfg.tune_steps = tune_steps
+        if tune_table:
+            arr = (_ffi.TuneEntry * len(tune_table))()
+            for q, e in enumerate(tune_table):
+                for k, _ in _ffi.TuneEntry._fields_:
+                    setattr(arr[q], k, int(e[k]))
+            cfg.tune_table = C.cast(arr, C.POINTER(_ffi.TuneEntry))
+            cfg.tune_entries = len(tune_table)
         self.precision = precision
         h = C.c_void_p()
         self._check(self.lib.lx_server_create(C.byref(cfg), C.byref(h)))

@@ -47,6 +47,14 @@ def step_bytes(p: Params) -> float:
     return b.value
 
 
+def trim_device_memory() -> None:
+    """Waits for the device and returns the memory pool's unused memory to the driver."""
+    lib = _ffi.lib()
+    st = lib.lx_trim_device_memory()
+    if st:
+        raise LuxumError(st, lib.lx_last_error(None).decode())
+
+
 def field_shape(p: Params, comp: int) -> tuple:
     """Staggered extent of a component for parameters p (host only)."""
     shp = (C.c_int * 3)()

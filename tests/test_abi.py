@@ -172,7 +172,7 @@ def test_ctypes_structs_match_the_header(tmp_path):
     if not cc:
         pytest.skip("no C compiler")
     structs = {"lx_params": _ffi.Params, "lx_request": _ffi.Request, "lx_server_config": _ffi.ServerConfig,
-               "lx_server_stats": _ffi.ServerStats, "lx_info": _ffi.Info}
+               "lx_server_stats": _ffi.ServerStats, "lx_info": _ffi.Info, "lx_tune_entry": _ffi.TuneEntry}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "luxum.h"', "int main(void) {"]
     for name, py in structs.items():
         lines.append(f'  printf("{name} %zu\\n", sizeof({name}));')

@@ -44,7 +44,7 @@ def _solo(name, steps, boxes, dft):
 def test_server_results_equal_solo(engine):
     from luxum_gb300 import Server
 
-    with Server(chunk=50) as srv:
+    with Server(chunk=50, tune_steps=5) as srv:
         ids = [srv.submit(_params(n), steps, boxes, dft) for n, steps, boxes, dft in REQS]
         for rid in ids:
             assert srv.wait(rid, 120.0) == "done", srv.error(rid)
@@ -77,13 +77,48 @@ def test_server_without_tuning_keeps_default_shapes(engine):
     from luxum_gb300 import Server
 
     n, steps, boxes, dft = REQS[0]
-    with Server(chunk=50, tune_steps=0) as srv:
+    with Server(chunk=50) as srv:  # no online tuning by default
         rid = srv.submit(_params(n), steps, boxes, dft)
         assert srv.wait(rid, 120.0) == "done", srv.error(rid)
         twin, plane = _solo(n, steps, boxes, dft)
         assert np.array_equal(srv.flux(rid), twin.dft_flux(plane))
         assert srv.tune_table() == [] and srv.stats()["tuned_classes"] == 0
         twin.close()
+
+
+def test_server_with_a_preset_table(engine):
+    """A table given at creation (say, from lx_batch_autotune on a sample of the expected
+    requests) shapes the server's launches from the first chunk; results stay bit-identical."""
+    from luxum_gb300 import Batch, Server, Sim
+
+    sample = [Sim(_params(n)) for n, _, _, _ in REQS]
+    b = Batch(chunk=10)
+    for s in sample:
+        b.add(s)
+    b.autotune(3)
+    table = b.tune_table()
+    b.close()
+    for s in sample:
+        s.close()
+    assert len(table) == 4
+    table = [dict(e, march=(2, 4, 1, 8)[q]) for q, e in enumerate(table)]  # shapes other than the default
+    with Server(chunk=50, tune_table=table) as srv:
+        assert srv.tune_table() == table
+        ids = [srv.submit(_params(n), steps, boxes, dft) for n, steps, boxes, dft in REQS]
+        for rid in ids:
+            assert srv.wait(rid, 120.0) == "done", srv.error(rid)
+        for rid, (n, steps, boxes, dft) in zip(ids, REQS):
+            twin, plane = _solo(n, steps, boxes, dft)
+            if dft is not None:
+                assert np.array_equal(srv.flux(rid), twin.dft_flux(plane))
+            assert srv.max_e2(rid) == twin.max_e2()
+            g = srv.take(rid, _params(n))
+            for c in range(6):
+                if np.prod(g.shape(c)):
+                    assert np.array_equal(g.field(c), twin.field(c)), (n, c)
+            g.close()
+            twin.close()
+        assert srv.stats()["tuned_classes"] == 0
 
 
 def test_server_arrivals_while_others_run(engine):
@@ -243,3 +278,22 @@ def test_fp16_storage_requests(engine):
     s.step(40)
     for c in range(6):
         assert np.array_equal(g.field(c), s.field(c)), c
+
+
+def test_trim_device_memory_after_teardown(engine):
+    """Destroyed handles give their memory back to the device pool; lx_trim_device_memory
+    returns it to the driver, and later handles allocate and step as before."""
+    from luxum_gb300 import Sim, trim_device_memory
+
+    n, steps, boxes, dft = REQS[1]
+    for s in [Sim(_params(n)) for _ in range(4)]:
+        s.step(3)
+        s.close()
+    trim_device_memory()
+    twin, _ = _solo(n, steps, boxes, dft)
+    again, _ = _solo(n, steps, boxes, dft)
+    for c in range(6):
+        if np.prod(again.shape(c)):
+            assert np.array_equal(again.field(c), twin.field(c))
+    twin.close()
+    again.close()
