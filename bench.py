@@ -446,7 +446,7 @@ def box_sims(n_sims: int, seed: int, precision: int, steps: int, side=(64, 192))
 
 
 def run_batch(n_sims: int, steps: int, three: bool, runs: int, solo_sample: int, solo_steps: int, peak: float,
-              peak_kind: str, side=(64, 192)) -> dict:
+              peak_kind: str, side=(64, 192), march_fixed: int = 0) -> dict:
     """Uneven simulations stepped as one batch: planar lenses, or 3-D cubes (three)."""
     import torch
 
@@ -459,7 +459,11 @@ def run_batch(n_sims: int, steps: int, three: bool, runs: int, solo_sample: int,
     for s in sims:
         batch.add(s)
     t_tune = time.perf_counter()
-    march = batch.autotune(20)  # tile shape timed on twins of the members, outside the timed region
+    if march_fixed:  # a given tile shape (profiling runs: no tuning launches before the steps)
+        batch.set_march(march_fixed, march_fixed)
+        march = (march_fixed, march_fixed)
+    else:
+        march = batch.autotune(20)  # tile shape timed on twins of the members, outside the timed region
     t_tune = time.perf_counter() - t_tune
 
     def run():
@@ -517,7 +521,7 @@ def bench_batch(args):
     peak, kind = measured_peaks()
     print(json.dumps(run_batch(args.batch_sims, args.batch_steps, args.config == "batch3d", args.steps,
                                args.solo_sample, args.solo_steps, peak, kind,
-                               (args.batch_side_lo, args.batch_side_hi))), flush=True)
+                               (args.batch_side_lo, args.batch_side_hi), args.batch_march)), flush=True)
 
 
 def serve_requests(n: int, seed: int, rate: float):
@@ -938,6 +942,8 @@ def main():
                     help="drop-in: the headline 256^3 FP64 workload; batch: 256 uneven planar simulations")
     ap.add_argument("--batch-sims", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=3000)
+    ap.add_argument("--batch-march", type=int, default=0, choices=[0, 1, 2, 4, 8],
+                    help="tile shape of the batched kernels (0: autotune before the timed steps)")
     ap.add_argument("--solo-sample", type=int, default=16)
     ap.add_argument("--solo-steps", type=int, default=300)
     ap.add_argument("--serve-requests", type=int, default=1000)
