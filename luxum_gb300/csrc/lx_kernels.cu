@@ -901,10 +901,15 @@ __global__ void __launch_bounds__(256) h_batch_2d(const StepParams<T, C>* __rest
   }
 }
 
-// (Capped at 8 blocks per SM, 32 registers: left to itself the compiler took 40 for this
-// kernel once the interior path prefetched, which leaves 6 blocks.)
+// With float compute capped at 8 blocks per SM, 32 registers: left to itself the compiler took
+// 40 for this kernel once the interior path prefetched, which leaves 6 blocks.  FP64 (doubles
+// take register pairs) is left uncapped: at 32 registers it spilled 48 bytes.
+template <class C>
+struct E2BatchMinBlocks {
+  static constexpr int v = sizeof(C) == 4 ? 8 : 1;
+};
 template <class T, class C, bool UNI, int M>
-__global__ void __launch_bounds__(256, 8) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
+__global__ void __launch_bounds__(256, E2BatchMinBlocks<C>::v) e_batch_2d(const StepParams<T, C>* __restrict__ ps, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   const StepParams<T, C>& p = ps[tl.x];
   const int k = tl.w + threadIdx.x;
