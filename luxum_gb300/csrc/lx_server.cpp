@@ -16,17 +16,17 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
-#include <array>
 #include <map>
-#include <set>
 #include <memory>
 #include <mutex>
 #include <new>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -388,10 +388,14 @@ extern "C" LX_API lx_status lx_server_create(const lx_server_config* cfg, lx_ser
   if (!st) st = lx_batch_set_chunk(srv->batch, c.chunk);
   if (!st && c.tune_entries > 0) {
     st = lx_batch_set_tune_table(srv->batch, c.tune_table, c.tune_entries);
+    int n = 0;
+    if (!st) st = lx_batch_get_tune_table(srv->batch, nullptr, 0, &n);  // the batch's copy: one entry per class
     if (!st) {
-      srv->table.assign(c.tune_table, c.tune_table + c.tune_entries);
-      for (const auto& e : srv->table) srv->tried.insert({e.planar, e.size_class, e.precision, e.slab_class});
+      srv->table.resize(n);
+      st = lx_batch_get_tune_table(srv->batch, srv->table.data(), n, &n);
     }
+    if (!st)
+      for (const auto& e : srv->table) srv->tried.insert({e.planar, e.size_class, e.precision, e.slab_class});
   }
   srv->cfg.tune_table = nullptr;  // copied: the caller's array need not outlive the call
   srv->cfg.tune_entries = 0;
