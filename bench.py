@@ -681,6 +681,23 @@ def run_serve(n_requests: int, rate: float, budget_gb: float, chunk: int, peak: 
             "dtype": "f32", "clocks": clk.summary()}
 
 
+def serve_in_child(n_requests: int, rate: float, budget_gb: float, chunk: int) -> dict:
+    """The serving stream in a process of its own, as a server runs in deployment.  Run after the
+    other workloads in this process, the stream's handle creation slowed threefold and its rate
+    fell 10-15 % (the cause is not identified; the twins of a batch tuner are enough to show it)."""
+    import subprocess
+
+    cmd = [sys.executable, os.path.abspath(__file__), "--config", "serve", "--serve-requests", str(n_requests),
+           "--serve-rate", str(rate), "--serve-budget-gb", str(budget_gb), "--serve-chunk", str(chunk)]
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=1800)
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    if out.returncode != 0 or not lines:
+        raise RuntimeError(f"serving child failed ({out.returncode}): {out.stderr[-2000:]}")
+    d = json.loads(lines[-1])
+    d["process"] = "its own (a child of the bench process)"
+    return d
+
+
 def bench_serve(args):
     """--config serve: the full request stream (1000 requests by default)."""
     import __graft_entry__
@@ -1146,8 +1163,8 @@ def main():
             "planar_512_fp64": run_planar(5, peak_bw, peak_kind),
             "phc_precision_study": run_phc(peak_bw, peak_kind),
             "lens_batch_fp32": run_batch(256, 3000, False, 1, args.solo_sample, args.solo_steps, peak_bw, peak_kind),
-            "serving_stream": run_serve(args.suite_serve_requests, args.serve_rate, args.serve_budget_gb,
-                                        args.serve_chunk, peak_bw, peak_kind)}
+            "serving_stream": serve_in_child(args.suite_serve_requests, args.serve_rate, args.serve_budget_gb,
+                                             args.serve_chunk)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         cpu = cpu_info(threads)
