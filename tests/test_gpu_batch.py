@@ -220,6 +220,28 @@ def test_tune_table_validation_and_member_tuning(engine):
     batch.close()
 
 
+def test_tune_table_errors(engine):
+    """Tuning a handle of another precision than the batch's members is refused; an empty
+    table clears the batch's picks; a batch without batched members tunes nothing."""
+    from luxum_gb300 import Batch, LuxumError
+
+    batch = Batch(chunk=10)
+    m = _make("planar_pml_axis", 1)
+    batch.add(m)
+    s64 = _make("planar_pml_axis", 0)
+    with pytest.raises(LuxumError):
+        batch.tune_member(s64, 3)
+    k = m.tune_class()
+    batch.set_tune_table([dict(k, march=2)])
+    assert batch.tune_table() == [dict(k, march=2)]
+    batch.set_tune_table([])
+    assert batch.tune_table() == []
+    batch.remove(m)
+    assert batch.autotune(3) == batch.march()  # nothing to time: the per-dimension march stays
+    assert batch.tune_table() == []
+    batch.close()
+
+
 def test_batch_autotune_leaves_members_untouched(engine):
     from luxum_gb300 import Batch
 

@@ -297,3 +297,19 @@ def test_trim_device_memory_after_teardown(engine):
             assert np.array_equal(again.field(c), twin.field(c))
     twin.close()
     again.close()
+
+
+def test_server_config_validation(engine):
+    """A table count without a table, and negative tuning steps, are refused at creation."""
+    import ctypes as C
+
+    from luxum_gb300 import _ffi
+
+    lib = _ffi.lib()
+    for field, value in (("tune_entries", 2), ("tune_steps", -1)):
+        cfg = _ffi.ServerConfig()
+        lib.lx_server_config_init(C.byref(cfg))
+        setattr(cfg, field, value)
+        h = C.c_void_p()
+        assert lib.lx_server_create(C.byref(cfg), C.byref(h)) == 1  # LX_ERR_INVALID
+        assert not h.value
