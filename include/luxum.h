@@ -265,8 +265,10 @@ LX_API lx_status lx_hdf5_read(const char* path, const char* dataset, double* out
  * all of them, one launch for every member's DFT planes and a step-counter tick.  3-D
  * members of 2^18 cells or more instead take one H and one E launch each, spread over four
  * streams so that they overlap.  Members are updated in place (planar FP32/FP16 handles
- * move their state into their first buffer on joining).  Chunks of
- * steps are captured once as a CUDA graph and replayed.  All members share one precision;
+ * move their state into their first buffer on joining).  From the second chunk
+ * after a change of members on, chunks of steps are captured once as a CUDA graph and replayed
+ * (the first is launched directly, so that a batch whose members change every chunk never
+ * waits for a capture).  All members share one precision;
  * members may not have snapshot outputs or probes (use lx_sim_step for those).  max|E|^2
  * is monitored every step.  A handle belongs to at most one batch; lx_sim_step on a member
  * is allowed between batch steps (the batch re-reads its step counter). */
@@ -333,7 +335,8 @@ LX_API lx_status lx_batch_tune_member(lx_batch* b, const lx_sim* sim, int steps,
 typedef struct lx_server lx_server;
 typedef struct lx_server_config {
   int precision;          /* LX_PREC_* shared by every request (default FP32) */
-  int chunk;              /* steps per batch launch, captured as a CUDA graph (default 100) */
+  int chunk;              /* steps per batch launch (default 100; captured as a CUDA graph when the
+                             members did not change since the last chunk) */
   double budget_bytes;    /* device memory for running requests (default 0: 90% of free) */
   int max_running;        /* 0: no limit besides the budget */
   int tune_steps;         /* > 0: tune each new class of batched request on twins of it before

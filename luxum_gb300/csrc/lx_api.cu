@@ -1858,6 +1858,7 @@ struct lx_batch {
   long long step = 0;  // batch steps taken (DFT sampling classes are phases of it)
   cudaGraphExec_t exec = nullptr;
   int exec_steps = 0;
+  long long chunks_since_rebuild = 0;  // a chunk is captured only when the one before had the same members
   long long exec_base_mod = -1;
   bool graphable = true;
   std::vector<int> host_ts;
@@ -2207,10 +2208,22 @@ static lx_status batch_run_async(lx_batch* b, int nsteps) {
   if (b->dirty || moved) {
     for (auto* s : b->sims) BCK(cudaStreamSynchronize(s->stream));  // members' own pending work first
     if ((st = batch_rebuild<T, C>(b))) return st;
+    b->chunks_since_rebuild = 0;
   }
   int done = 0;
   if (b->chunk > 0 && b->graphable) {
     while (nsteps - done >= b->chunk) {
+      // The first chunk after a change of members is launched directly: capturing and
+      // instantiating a graph is host time before any of its work starts, while direct
+      // launches run as they are issued.  A serving loop whose members change every chunk
+      // never captures (1000-request stream: 55.4 -> 61.0 Gcell/s); a steady batch replays
+      // a graph from its second chunk on.
+      if (b->chunks_since_rebuild++ == 0) {
+        if ((st = batch_enqueue<T, C>(b, b->step, b->chunk))) return st;
+        b->step += b->chunk;
+        done += b->chunk;
+        continue;
+      }
       const long long base_mod = b->step % b->chunk;
       if (!b->exec || b->exec_steps != b->chunk || b->exec_base_mod != base_mod) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -2235,6 +2248,7 @@ static lx_status batch_run_async(lx_batch* b, int nsteps) {
   if (nsteps - done > 0) {
     if ((st = batch_enqueue<T, C>(b, b->step, nsteps - done))) return st;
     b->step += nsteps - done;
+    b->chunks_since_rebuild++;
   }
   for (size_t q = 0; q < b->sims.size(); q++) {
     b->sims[q]->t += nsteps;
