@@ -2,10 +2,10 @@
 
 Stated tolerances (relative L2 per field component, relative to its field group's norm as
 in cases.field_errors, after the case's step count):
-  FP32 (fields, psi and coefficients in FP32; profiles and TF/SF tables evaluated in FP64):
-       <= 1e-4 (spec bar for the FP32 form)
+  FP32 (fields, psi and coefficients in FP32; profiles and TF/SF positions in FP64, the
+       TF/SF exponential in FP32): <= 1e-4, the bound the FP32 form is held to
   FP16 storage / FP32 compute (E, H stored as binary16):
-       <= 3e-2 (stated error of the storage format; no bar in the benchmark spec)
+       <= 3e-2 (the storage format's own error; the form is held to no tighter bound)
 """
 import numpy as np
 import pytest
