@@ -428,8 +428,17 @@ __device__ __forceinline__ typename MaxBits<C>::type e_cell_3d(const StepParams<
   return e_apply<T, C, UNI, MON, FAST>(p, i, j, k, tf, v);
 }
 
+// Resident blocks per SM asked of the compiler for the 3-D E kernel: FP16 storage takes 8 (32
+// registers, about 30 bytes spilled) together with the interior fast path, 0.3196 -> 0.3116 ms
+// per 256^3 step (each alone was slower: the fast path 0.332, the cap 0.356); FP32 storage runs
+// best at the compiler's own 40 (the cap cost it 4 %), and FP64 is bound by its pipe.
+template <class T>
+struct EMinBlocks {
+  static constexpr int v = sizeof(T) == 2 ? 8 : 0;
+};
+
 template <class T, class C, bool UNI, bool MON, int ZW>
-__global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
+__global__ void __launch_bounds__(256, EMinBlocks<T>::v) e_kernel_3d(const StepParams<T, C> p) {
   constexpr int RY = 256 / ZW;
   const ZTile z = z_tile<ZW>(p.Nz, p.zends);
   const int k = z.k;
@@ -437,9 +446,9 @@ __global__ void __launch_bounds__(256) e_kernel_3d(const StepParams<T, C> p) {
   const int i = blockIdx.z;
   const bool tf = p.tfsf && ztile_meets_planes(p.planesE, i, blockIdx.y * RY, RY, z);
   typename MaxBits<C>::type mbits = 0;
-  // The interior fast path pays for FP32 storage only (1.5 %); FP64 is bound by its pipe
-  // either way, and FP16 storage ran 9 % slower with it.
-  constexpr bool kFast = sizeof(T) == 4;
+  // The interior fast path pays for float compute (FP16 storage with the register cap above);
+  // FP64 is bound by its pipe either way.
+  constexpr bool kFast = sizeof(T) < 8;
   if (z.valid && j < p.Ny) {
     if (kFast && !tf && z.n1 == 0 && tile_is_interior(p.slab, p.pml, p.Nx, p.Ny, p.Nz, i, 1, blockIdx.y * RY, RY, z.lo0, z.n0))
       mbits = e_cell_3d<T, C, UNI, MON, kFast>(p, i, j, k, false);
